@@ -1,0 +1,375 @@
+#!/usr/bin/env python3
+"""Cloud raymarch throughput at 3840x2160: Mrays/s and ms/frame.
+
+One step = one full 3840x2160 frame of the cloud march (every pixel marched), cycling through the
+16-frame camera sweep (yaw 0 -> 90 deg, pitch 5 -> 25 deg, t += 0.1 s; sun 30 deg) over the seed-0
+textures that mm_noise_generate makes on the GPU.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Our arm times K frames with CUDA events on the launch stream (L2 flushed between frames by a
+256 MB memset outside the events), takes the max over ranks, and prints one JSON line with the
+end-to-end figure through the C ABI (host-visible output copied back every frame), the roofline
+of the march kernel against the on-chip rates it is bound by, the sampled SM clocks and a CPU
+baseline (the FP32 oracle on the host cores over a sample of the same frames).
+The reference arm (--impl reference) times the reference's march on the host CPU: the FP32
+oracle restatement of compute-clouds.comp over all host threads, one bounded sample per step.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for _p in (REPO, os.path.join(REPO, "project-marshmallow_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "Mrays/s at 3840x2160 (cloud raymarch frame, every pixel marched)"
+SWEEP = 16
+PROFILE_SUMMARY = os.path.join(REPO, "profiles", "march_kernel_4k.txt")
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=48)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--width", type=int, default=3840)
+    ap.add_argument("--height", type=int, default=2160)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def rank_info():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+# ------------------------------------------------------------------------------ clocks
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples taken while the timed region runs."""
+
+    FIELDS = ("index,uuid,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, uuid):
+        self.uuid = uuid
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                                          "-lms", "50"], stdout=self.out, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.close()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 10:
+                continue
+            if self.uuid and self.uuid not in f[1]:
+                continue
+            rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        mhz = sorted(float(r[2]) for r in rows if r[2].replace(".", "").isdigit())
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[6 + i].lower() == "active"})
+        return {"sm_mhz": mhz[len(mhz) // 2] if mhz else None,
+                "sm_max_mhz": float(rows[0][3]) if rows[0][3].replace(".", "").isdigit() else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------------------------ shared
+
+
+def sweep(k):
+    import marshmallow as mm
+    return mm.scene.sweep_params(k % SWEEP, SWEEP)
+
+
+def frame_uniforms(k, w, h):
+    import marshmallow as mm
+    return mm.scene.sweep_uniforms(k % SWEEP, w, h, n=SWEEP)
+
+
+def cpu_march_sample(u, host_tex, w, h, row0, step):
+    """FP32 oracle over rows row0::step and columns row0%step::step; returns (rays, seconds, threads)."""
+    import oracle
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    rgba, _, _ = oracle.march(u, host_tex, w, h, precision=32, rows=(row0, h, step), col_begin=row0 % step,
+                              col_step=step, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return rgba.shape[0] * rgba.shape[1], dt, threads
+
+
+def oracle_textures():
+    import oracle
+    import marshmallow.lib as L
+    return {"low_res": oracle.noise(L.NOISE_LOWRES, 0, 128, 128, 128, 4),
+            "hi_res": oracle.noise(L.NOISE_HIRES, 0, 32, 32, 32, 4),
+            "curl": oracle.noise(L.NOISE_CURL2D, 0, 128, 128, 1, 2)[0],
+            "weather": oracle.noise(L.NOISE_WEATHER, 0, 512, 512, 1, 4)[0]}
+
+
+# ------------------------------------------------------------------------------ reference arm
+
+
+def run_reference(args):
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return
+    import oracle
+    oracle.build()
+    w, h = args.width, args.height
+    tex = oracle_textures()
+    step_px = 8  # each step: 1/64 of the frame (every 8th row and column), a bounded CPU sample
+    for k in range(args.warmup):
+        cpu_march_sample(frame_uniforms(k, w, h), tex, w, h, k % step_px, step_px)
+    rays = 0
+    secs = 0.0
+    threads = 1
+    for k in range(args.steps):
+        n, dt, threads = cpu_march_sample(frame_uniforms(k, w, h), tex, w, h, k % step_px, step_px)
+        rays += n
+        secs += dt
+    value = rays / secs / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mrays/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * secs / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "cloud march %dx%d, 16-frame sweep, seed-0 textures" % (w, h), "width": w,
+                   "height": h, "sample_per_step": "every 8th row and column of one frame (1/64 of its rays)"},
+        "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": "FP32 oracle restatement of compute-clouds.comp; per step 1/64 of a 4K frame"},
+        "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------------------ our arm
+
+
+def read_profile_traffic():
+    """Per-launch DRAM bytes of the march kernel from the committed ncu summary, if present."""
+    try:
+        for line in open(PROFILE_SUMMARY):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def run_ours(args):
+    import torch
+    import marshmallow as mm
+    import marshmallow.lib as L
+
+    rank, world, local = rank_info()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    lib = L.load()
+    w, h = args.width, args.height
+    stream = torch.cuda.current_stream()
+    sptr = C.c_void_p(stream.cuda_stream)
+
+    textures = mm.render.Textures(seed=0)
+    renderer = mm.render.Renderer()
+    rgba = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+    depth = torch.empty((h, w), dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    uniforms = [frame_uniforms(k, w, h) for k in range(SWEEP)]
+
+    def march(k, out_rgba=rgba, out_depth=depth, s=None, counters=None):
+        renderer.march(uniforms[k % SWEEP], textures, out_rgba, out_depth, stream=s, counters=counters)
+
+    for k in range(args.warmup):
+        march(k)
+    torch.cuda.synchronize()
+
+    props = torch.cuda.get_device_properties(local)
+    uuid = str(getattr(props, "uuid", "") or "")
+    sampler = ClockSampler(uuid)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    launches0 = lib.mm_kernel_launch_count()
+    for k in range(args.steps):
+        flush.zero_()  # L2 flush between frames, outside the timed events
+        ev[k][0].record(stream)
+        march(k)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    launches = lib.mm_kernel_launch_count() - launches0
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(step_ms)
+    if dist:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    rays_per_frame = w * h
+    value = world * rays_per_frame * args.steps / (total_ms * 1e-3) / 1e6
+    ms_frame = total_ms / args.steps
+
+    # Algorithmic work of the timed frames (same frames, counted in a separate untimed pass).
+    cnt = torch.zeros(4, dtype=torch.int64, device="cuda")
+    for k in range(args.steps):
+        march(k, counters=cnt)
+    torch.cuda.synchronize()
+    n_test, n_hires, n_iter, n_acc = (int(x) for x in cnt.cpu().tolist())
+    f3d = (n_test + n_hires) / args.steps  # trilinear 3D fetches per frame (one per call)
+    f2d = (n_test + n_hires) / args.steps  # bilinear 2D fetches per frame (one per call)
+
+    # On-chip peaks measured now on this GPU (MEASURED_PEAKS.json holds HBM and bf16 only).
+    pk = (C.c_double * 3)()
+    L.check(lib.mm_measure_peaks(textures.handles["low_res"], textures.handles["weather"], pk, sptr),
+            "mm_measure_peaks")
+    peak3d, peak2d, peak_fp32 = pk[0], pk[1], pk[2]
+    sec_frame = ms_frame * 1e-3
+    tex_time_frac = (f3d / (peak3d * 1e9) + f2d / (peak2d * 1e9)) / sec_frame
+    achieved_gfetch = (f3d + f2d) / sec_frame / 1e9
+    # UNORM8 texel bytes: 8 x 4 B per trilinear RGBA fetch, 4 x 4 B per bilinear weather fetch,
+    # 4 x 2 B per bilinear RG curl fetch.
+    texel_bytes = 32.0 * f3d + (16.0 * n_test + 8.0 * n_hires) / args.steps
+    peak_eff = (f3d + f2d) / (f3d / peak3d + f2d / peak2d) if f3d + f2d > 0 else peak3d
+    out_bytes = 20.0 * rays_per_frame  # RGBA32F + depth written once
+    peaks_file = os.path.join(REPO, "MEASURED_PEAKS.json")
+    hbm_peak = None
+    if os.path.exists(peaks_file):
+        hbm_peak = json.load(open(peaks_file)).get("hbm_gbs")
+    hbm_achieved = (out_bytes + 9.4e6) / sec_frame / 1e9
+    traffic = read_profile_traffic()
+
+    # End to end through the C ABI with host buffers: each frame's uniforms go to the device with the
+    # launch (mm_uniforms by value), the frame's RGBA32F + depth come back to pinned host memory.
+    e2e = None
+    if not args.no_e2e:
+        s_cmp = torch.cuda.Stream()
+        s_cpy = torch.cuda.Stream()
+        dev_rgba = [rgba, torch.empty_like(rgba)]
+        dev_depth = [depth, torch.empty_like(depth)]
+        host_rgba = [torch.empty((h, w, 4), dtype=torch.float32, pin_memory=True) for _ in range(2)]
+        host_depth = [torch.empty((h, w), dtype=torch.float32, pin_memory=True) for _ in range(2)]
+        done_cmp = [torch.cuda.Event() for _ in range(2)]
+        done_cpy = [torch.cuda.Event() for _ in range(2)]
+        for i in range(2):
+            done_cpy[i].record(s_cpy)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            b = k % 2
+            s_cmp.wait_event(done_cpy[b])
+            march(k, dev_rgba[b], dev_depth[b], s=s_cmp)
+            done_cmp[b].record(s_cmp)
+            s_cpy.wait_event(done_cmp[b])
+            with torch.cuda.stream(s_cpy):
+                host_rgba[b].copy_(dev_rgba[b], non_blocking=True)
+                host_depth[b].copy_(dev_depth[b], non_blocking=True)
+            done_cpy[b].record(s_cpy)
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        if dist:
+            t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e = {"value": round(world * rays_per_frame * args.steps / e2e_s / 1e6, 3), "unit": "Mrays/s",
+               "h2d_bytes_per_step": C.sizeof(L.Uniforms), "d2h_bytes_per_step": 20 * rays_per_frame,
+               "ms_per_step": round(1e3 * e2e_s / args.steps, 3)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import oracle
+        oracle.build()
+        host_tex = textures.host_all()
+        rays = 0
+        secs = 0.0
+        threads = 1
+        for k in (0, 8):  # two sweep frames, every 4th row and column
+            n, dt, threads = cpu_march_sample(uniforms[k], host_tex, w, h, k % 4, 4)
+            rays += n
+            secs += dt
+        cpu = {"value": round(rays / secs / 1e6, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+               "sample": "FP32 oracle restatement of compute-clouds.comp on frames 0 and 8 of the sweep, every "
+                         "4th row and column (%d rays, %.1f s)" % (rays, secs)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_frame, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "cloud march %dx%d, plain FP32, hardware-filtered UNORM8 textures, "
+                                   "16-frame sweep" % (w, h),
+                       "width": w, "height": h, "frames_cycled": SWEEP, "textures": "seed 0, generated on GPU",
+                       "l2": "flushed between frames (256 MB memset outside the timed events)",
+                       "variant": "plain", "math": "fast", "sampler": "hardware"},
+            "roofline": {"bound": "tex", "achieved": round(achieved_gfetch, 2), "peak": round(peak_eff, 1),
+                         "unit": "Gfetch/s",
+                         "frac": round(tex_time_frac, 4), "traffic": traffic,
+                         "peak_3d_gfetch": round(peak3d, 1), "peak_2d_gfetch": round(peak2d, 1),
+                         "fetches_3d_per_frame": f3d, "fetches_2d_per_frame": f2d,
+                         "texel_bytes_per_frame": texel_bytes,
+                         "peak_source": "in-run microbenchmark mm_measure_peaks (texture unit, L1-resident)",
+                         "frac_definition": "time the texture unit needs at its measured peak for the frame's "
+                                            "algorithmic fetches / kernel time"},
+            "roofline_hbm": {"bound": "hbm", "achieved": round(hbm_achieved, 2), "peak": hbm_peak, "unit": "GB/s",
+                             "frac": round(hbm_achieved / hbm_peak, 4) if hbm_peak else None,
+                             "algorithmic_bytes": out_bytes + 9.4e6, "traffic": traffic},
+            "fp32_peak_tflops": round(peak_fp32, 2),
+            "work_per_frame": {"cloud_test": n_test / args.steps, "cloud_hires": n_hires / args.steps,
+                               "iterations": n_iter / args.steps, "accumulated": n_acc / args.steps},
+            "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks, "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    renderer.close()
+    textures.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

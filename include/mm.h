@@ -1,0 +1,276 @@
+/*
+ * mm.h - C ABI of the GB300 cloud raymarch pass and its noise-texture generators.
+ *
+ * This library replaces one Vulkan compute pass of Project-Marshmallow: the cloud raymarch shader
+ * SkyEngine/SkyEngine/Shaders/compute-clouds.comp, its descriptor contract
+ * (SkyEngine/SkyEngine/Shader.cpp:662-693) and its dispatch
+ * (SkyEngine/SkyEngine/VulkanApplication.cpp:1062-1071), plus the textures that feed it.
+ *
+ * Conventions
+ *  - Every entry point returns an mm_status; none throws or aborts.  mm_last_error_string()
+ *    describes the most recent failure of the calling thread.
+ *  - Device work is stream ordered and asynchronous.  `stream` is a cudaStream_t passed as void*
+ *    (NULL = the legacy default stream).
+ *  - Device pointers are plain CUDA device pointers owned by the caller unless stated otherwise.
+ *  - Matrices are column-major float[16] (glm / GLSL layout), element [col*4 + row].
+ */
+#ifndef MM_H_
+#define MM_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MM_ABI_VERSION 1
+
+typedef enum mm_status {
+    MM_OK = 0,
+    MM_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad size, bad enum, wrong texture shape */
+    MM_ERR_CUDA = 2,             /* a CUDA runtime call failed (text in mm_last_error_string) */
+    MM_ERR_OUT_OF_MEMORY = 3,    /* a device or host allocation failed */
+    MM_ERR_UNSUPPORTED = 4,      /* valid request this build does not implement */
+    MM_ERR_TIMEOUT = 5,          /* a bounded device-side wait gave up */
+    MM_ERR_NO_DEVICE = 6         /* no usable CUDA device */
+} mm_status;
+
+/* ------------------------------------------------------------------------------------------ */
+/* Uniform blocks.  Byte layout = std140 layout of the shader's UBOs                           */
+/* (compute-clouds.comp:12-41; host structs Shader.h:24-28, SkyManager.h:8-37).               */
+/* ------------------------------------------------------------------------------------------ */
+
+/* UniformCameraObject (Shader.h:24-28): 160 bytes. */
+typedef struct mm_camera_ubo {
+    float view[16];            /* world -> view; rows 0..2 of the 3x3 part = right, up, forward */
+    float proj[16];            /* perspective with proj[1][1] negated (VulkanApplication.cpp:362) */
+    float camera_position[4];  /* xyz = eye, w = 1 */
+    float camera_params[4];    /* x = aspect, y = tan(0.5 * 0.01745 * fov_deg) (camera.h:72) */
+} mm_camera_ubo;
+
+/* UniformCameraObjectPrev (compute-clouds.comp:19-23): 144 bytes; read only by reprojection. */
+typedef struct mm_camera_prev_ubo {
+    float view[16];
+    float proj[16];
+    float camera_position[4];
+} mm_camera_prev_ubo;
+
+/* UniformSunObject (SkyManager.h:8-15): 116 bytes of data, padded to 128 as std140 does. */
+typedef struct mm_sun_ubo {
+    float location[4];
+    float direction[4];
+    float color[4];            /* rgb = sun colour; a = pixel phase 0..15 of the 1/16 update */
+    float direction_basis[16]; /* columns: N, sun direction, B (SkyManager.cpp:46-70) */
+    float intensity;
+    float pad_[3];
+} mm_sun_ubo;
+
+/* UniformSkyObject (SkyManager.h:28-37): 52 bytes of data, padded to 64. */
+typedef struct mm_sky_ubo {
+    float beta_r[4];
+    float beta_v[4];
+    float wind[4];             /* xyz = wind direction, w = time */
+    float mie_directional;
+    float pad_[3];
+} mm_sky_ubo;
+
+/* All four blocks of descriptor set 2 bindings 0..3, in binding order (496 bytes). */
+typedef struct mm_uniforms {
+    mm_camera_ubo camera;
+    mm_camera_prev_ubo camera_prev;
+    mm_sun_ubo sun;
+    mm_sky_ubo sky;
+} mm_uniforms;
+
+/* ------------------------------------------------------------------------------------------ */
+/* Host scene set-up: camera and sky math of camera.cpp / SkyManager.cpp, restated.            */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Camera from eye position and angles.  The march casts rays along -m_forward
+ * (compute-clouds.comp:312-322 with camera.cpp:27-39), so `pitch_deg`/`yaw_deg` give the
+ * direction the image centre looks at: d = (cos yaw cos pitch, sin pitch, sin yaw cos pitch)
+ * and m_forward = -d; right/up follow camera.cpp:139-148.  `fov_deg` is the vertical field of
+ * view converted with DEG2RAD = 0.01745 (camera.h:15,72).  camera_prev is set equal to camera. */
+int mm_camera_from_angles(const float eye[3], float yaw_deg, float pitch_deg, float fov_deg,
+                          int width, int height, mm_uniforms* u);
+
+/* Sun/sky blocks from a sun direction given as elevation/azimuth in degrees:
+ * dir = (cos el cos az, sin el, cos el sin az), then the TBN, intensity, colour and
+ * scattering coefficients of SkyManager.cpp:15-70 (SkyManager::calcSun*, calcSkyBeta*).
+ * wind = (1, 0.05, 1, time) (SkyManager.cpp:85-90); mie_directional = 0.8, rayleigh = 2,
+ * mie = 0.005, turbidity = 10.  sun.color.a = pixel_phase. */
+int mm_sky_from_sun_angles(float elevation_deg, float azimuth_deg, float time, int pixel_phase,
+                           mm_uniforms* u);
+
+/* Same blocks from SkyManager::rebuildSkyFromNewSun's fractional parameters
+ * (SkyManager.cpp:108-116, 46-52): theta = 2 pi (elevation - 0.5), phi = 2 pi (azimuth - 0.5). */
+int mm_sky_from_reference_fractions(float elevation, float azimuth, float time, int pixel_phase,
+                                    mm_uniforms* u);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Textures (replace Texture.cpp / Texture3D and the stb-loaded assets of                      */
+/* VulkanApplication.cpp:240-265).  Sampling follows the reference samplers: LINEAR filter,    */
+/* REPEAT wrap on every axis, normalized coordinates, mip level 0 only (Texture.cpp:29-52,     */
+/* 315-338).                                                                                   */
+/* ------------------------------------------------------------------------------------------ */
+
+typedef enum mm_noise_kind {
+    MM_NOISE_LOWRES_PERLIN_WORLEY = 0, /* 3D RGBA8: R Perlin-Worley, GBA Worley FBM (4/8/16 cells) */
+    MM_NOISE_HIRES_WORLEY = 1,         /* 3D RGBA8: RGB Worley FBM (2/4/8 cells), A = 0 */
+    MM_NOISE_CURL2D = 2,               /* 2D RG8: curl of 2D Perlin FBM (5 octaves) */
+    MM_NOISE_WEATHER = 3,              /* 2D RGBA8: R coverage, G 0, B cloud type, A 255 */
+    MM_NOISE_REF_CURL = 4              /* 2D RGBA8: ImageUtils.cpp GenerateCurlNoise (freq 3, 4 oct) */
+} mm_noise_kind;
+
+typedef enum mm_texel_format {
+    MM_FORMAT_UNORM8 = 0, /* texel/255, as VK_FORMAT_R8G8B8A8_UNORM (Texture.h:29) */
+    MM_FORMAT_FP16 = 1,   /* IEEE half, value = texel/255 rounded to half */
+    MM_FORMAT_BF16 = 2    /* bfloat16, value = texel/255 rounded to bf16 */
+} mm_texel_format;
+
+typedef struct mm_noise_desc {
+    int kind;       /* mm_noise_kind */
+    uint32_t seed;  /* ignored by MM_NOISE_REF_CURL, which has no seed */
+    int width;      /* texels per side; 0 = the kind's default size */
+    int height;
+    int depth;      /* 1 for 2D kinds */
+} mm_noise_desc;
+
+typedef struct mm_texture_s* mm_texture;
+
+/* Generates a noise texture on the GPU into a new library-owned texture (device texels plus
+ * a hardware texture object).  Default sizes: low-res 128^3, hi-res 32^3, curl 128^2,
+ * weather 512^2, reference curl 128^2.  Replaces the pre-baked TGA/PNG assets loaded at
+ * VulkanApplication.cpp:253-262. */
+int mm_noise_generate(const mm_noise_desc* desc, mm_texture* out, void* stream);
+
+/* Bytes of raw UNORM8 texels mm_noise_fill writes for `desc` (after defaults are applied). */
+int mm_noise_texel_bytes(const mm_noise_desc* desc, size_t* bytes);
+
+/* Writes the raw UNORM8 texels of a noise kind into caller device memory (x fastest, then y,
+ * then z; 4 bytes per texel, 2 for MM_NOISE_CURL2D).  No texture object is made.
+ * MM_NOISE_REF_CURL needs device scratch for its min/max normalisation and allocates it per
+ * call. */
+int mm_noise_fill(const mm_noise_desc* desc, void* d_texels, size_t bytes, void* stream);
+
+/* Hash stage of the seeded generators, for bit-exactness checks: out[i] = hash3(x, y, z, s) for
+ * the n int32 triples at d_xyz (device), with hash3(x,y,z,s) = h(x + h(y + h(z + s))) and h the
+ * lowbias32 integer mixer. */
+int mm_noise_hash3(const int32_t* d_xyz, uint32_t stream_seed, size_t n, uint32_t* d_out, void* stream);
+
+/* Hash stage of the reference curl generator: out[i] = hashNoise(x, y, z) of ImageUtils.cpp:25-29
+ * (fract(sinf(dot(p, (12.9898, 78.233, 47.387))) * 43758.5453)) for n float triples (device). */
+int mm_ref_curl_hash(const float* d_xyz, size_t n, float* d_out, void* stream);
+
+/* Creates a texture from UNORM8 texels already in caller memory (`src_is_device` 0 = host).
+ * channels is 1, 2 or 4; depth 1 makes a 2D texture.  `format` selects the storage of the
+ * hardware-filtered copy; the UNORM8 texels are always kept for software sampling. */
+int mm_texture_create(const void* texels, int src_is_device, int width, int height, int depth,
+                      int channels, int format, mm_texture* out, void* stream);
+
+/* Width/height/depth/channels/format of a texture. */
+int mm_texture_info(mm_texture tex, int* width, int* height, int* depth, int* channels,
+                    int* format);
+
+/* Copies the UNORM8 texels of a texture to host memory (synchronous). */
+int mm_texture_copy_to_host(mm_texture tex, void* dst, size_t bytes);
+
+/* Re-encodes the hardware-filtered copy of a texture in another mm_texel_format. */
+int mm_texture_set_format(mm_texture tex, int format, void* stream);
+
+int mm_texture_destroy(mm_texture tex);
+
+/* The five samplers of descriptor set 2 bindings 4..8 (compute-clouds.comp:43-47).
+ * night_sky may be NULL when the sun is above the horizon. */
+typedef struct mm_scene_textures {
+    mm_texture weather;   /* cloudPlacement, 2D */
+    mm_texture night_sky; /* nightSkyMap, 2D */
+    mm_texture curl;      /* curlNoise, 2D */
+    mm_texture low_res;   /* lowResCloudShape, 3D */
+    mm_texture hi_res;    /* hiResCloudShape, 3D */
+} mm_scene_textures;
+
+/* ------------------------------------------------------------------------------------------ */
+/* The cloud march (compute-clouds.comp:288-500).                                              */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Output images (set 0 binding 0 `resultImage`, rgba32f), plus a depth image the reference
+ * does not have: the march distance t of the first sample whose density is accumulated
+ * (compute-clouds.comp:466), +INF where no sample is accumulated. */
+typedef struct mm_image {
+    float* rgba;              /* device, width*height float4 rows */
+    size_t rgba_pitch_bytes;  /* >= 16*width, multiple of 16 */
+    float* depth;             /* device, may be NULL */
+    size_t depth_pitch_bytes; /* >= 4*width */
+    int width;
+    int height;
+} mm_image;
+
+typedef enum mm_pixel_mode {
+    MM_PIXELS_FULL = 0,   /* every pixel is marched */
+    MM_PIXELS_PHASE16 = 1 /* only pixels (4i + p%4, 4j + p/4), p = int(sun.color.a)
+                             (compute-clouds.comp:292-298); other pixels are untouched */
+} mm_pixel_mode;
+
+typedef enum mm_sampler_mode {
+    MM_SAMPLER_HARDWARE = 0, /* CUDA texture objects (8-bit fixed-point filter weights) */
+    MM_SAMPLER_SOFTWARE = 1  /* software trilinear/bilinear with float weights */
+} mm_sampler_mode;
+
+typedef enum mm_math_mode {
+    MM_MATH_FAST = 0,  /* FMA contraction and hardware transcendental approximations */
+    MM_MATH_EXACT = 1  /* IEEE +,-,*,/,sqrt without contraction and the library's own
+                          elementary functions: reproduces the FP32 CPU oracle bit for bit
+                          when combined with MM_SAMPLER_SOFTWARE */
+} mm_math_mode;
+
+typedef struct mm_march_options {
+    int pixel_mode;        /* mm_pixel_mode */
+    int sampler;           /* mm_sampler_mode */
+    int math;              /* mm_math_mode */
+    int density_format;    /* mm_texel_format of the hardware-filtered density textures */
+    float coverage_offset; /* added to weather.r before min(0.85, .) (0 = reference) */
+    int ref_uv_1080p;      /* 1: uv = pixel / (1920,1080) as the shader hard-codes
+                              (compute-clouds.comp:283-285,305); 0: uv = pixel / (width,height) */
+    uint64_t* d_counters;  /* optional device uint64[4]: cloudTest calls, cloudHiRes calls,
+                              loop iterations, accumulated samples (atomically added) */
+} mm_march_options;
+
+/* Fills `o` with the defaults: full frame, hardware sampler, fast math, UNORM8, offset 0,
+ * uv = pixel/(width,height), no counters. */
+int mm_march_options_default(mm_march_options* o);
+
+typedef struct mm_context_s* mm_context;
+
+/* A context owns the per-device scratch the march uses (work-queue counters).  Create it with
+ * the target device current.  Contexts must not be shared by concurrent streams. */
+int mm_context_create(mm_context* out);
+int mm_context_destroy(mm_context ctx);
+
+/* Renders one cloud frame (replaces vkCmdDispatch of the compute pipeline,
+ * VulkanApplication.cpp:1062-1071).  `u` is read on the host at call time (no device copy is
+ * kept).  Stream ordered; returns after the launch. */
+int mm_clouds_march(mm_context ctx, const mm_uniforms* u, const mm_scene_textures* tex,
+                    const mm_image* out, const mm_march_options* opt, void* stream);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Diagnostics                                                                                 */
+/* ------------------------------------------------------------------------------------------ */
+
+const char* mm_last_error_string(void);
+int mm_abi_version(void);
+/* Number of device kernels this library has launched since load (all entry points). */
+uint64_t mm_kernel_launch_count(void);
+
+/* Measures the on-chip rates the march is bound by, on the current device:
+ * out[0] trilinear 3D filtered fetches (G/s) from `tex3d`, out[1] bilinear 2D filtered fetches
+ * (G/s) from `tex2d` (both RGBA textures with texture objects), out[2] FP32 FMA throughput
+ * (TFLOP/s).  Synchronizes `stream`.  No reference counterpart (the reference has no timing). */
+int mm_measure_peaks(mm_texture tex3d, mm_texture tex2d, double* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MM_H_ */

@@ -1,0 +1,123 @@
+"""ctypes binding of the CPU oracle (oracle/_build/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: the parity tests, the smoke check and the CPU-baseline leg of bench.py
+use it as the checker.  The library (project-marshmallow_gb300) never imports it.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+ORACLE_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(ORACLE_DIR, "_build", "liboracle.so")
+
+_lib = None
+
+
+class OracleTexture(C.Structure):
+    _fields_ = [("texels", C.c_void_p), ("width", C.c_int), ("height", C.c_int), ("depth", C.c_int),
+                ("channels", C.c_int)]
+
+
+class OracleTextures(C.Structure):
+    _fields_ = [("weather", OracleTexture), ("night_sky", OracleTexture), ("curl", OracleTexture),
+                ("low_res", OracleTexture), ("hi_res", OracleTexture)]
+
+
+class OracleFrame(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("pixel_mode", C.c_int), ("coverage_offset", C.c_float),
+                ("ref_uv_1080p", C.c_int), ("row_begin", C.c_int), ("row_end", C.c_int), ("row_step", C.c_int),
+                ("col_begin", C.c_int), ("col_step", C.c_int)]
+
+
+def build():
+    """Compiles liboracle.so with the committed Makefile (idempotent)."""
+    subprocess.run(["make", "-s", "-C", ORACLE_DIR, "_build/liboracle.so"], check=True)
+    return LIB
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        lib = C.CDLL(LIB)
+        lib.oracle_march_f32.argtypes = [C.c_void_p, C.POINTER(OracleTextures), C.POINTER(OracleFrame), C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_int]
+        lib.oracle_march_f64.argtypes = lib.oracle_march_f32.argtypes
+        lib.oracle_ref_curl.argtypes = [C.c_void_p]
+        lib.oracle_ref_curl_hash_index.argtypes = [C.c_float, C.c_float, C.c_float]
+        lib.oracle_ref_curl_hash.argtypes = [C.c_float, C.c_float, C.c_float]
+        lib.oracle_ref_curl_hash.restype = C.c_float
+        lib.oracle_mm_math.argtypes = [C.c_int, C.c_float, C.c_float]
+        lib.oracle_mm_math.restype = C.c_float
+        lib.oracle_noise_fill.argtypes = [C.c_int, C.c_uint32, C.c_int, C.c_int, C.c_int, C.c_void_p]
+        lib.oracle_hash32.argtypes = [C.c_uint32]
+        lib.oracle_hash32.restype = C.c_uint32
+        lib.oracle_hash3.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_uint32]
+        lib.oracle_hash3.restype = C.c_uint32
+        lib.oracle_tonemap.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p]
+        _lib = lib
+    return _lib
+
+
+def noise(kind, seed, w, h, d, channels):
+    """Texels of a seeded generator as a (d, h, w, channels) uint8 array."""
+    out = np.zeros((d, h, w, channels), np.uint8)
+    rc = load().oracle_noise_fill(kind, seed, w, h, d, out.ctypes.data)
+    if rc:
+        raise RuntimeError("oracle_noise_fill failed: %d" % rc)
+    return out
+
+
+def ref_curl():
+    out = np.zeros((128, 128, 4), np.uint8)
+    rc = load().oracle_ref_curl(out.ctypes.data)
+    if rc:
+        raise RuntimeError("oracle_ref_curl failed: %d" % rc)
+    return out
+
+
+def _tex(a):
+    if a is None:
+        return OracleTexture(None, 0, 0, 0, 0)
+    a = np.ascontiguousarray(a)
+    if a.ndim == 3:  # 2D texture (h, w, c)
+        return OracleTexture(a.ctypes.data, a.shape[1], a.shape[0], 1, a.shape[2])
+    return OracleTexture(a.ctypes.data, a.shape[2], a.shape[1], a.shape[0], a.shape[3])
+
+
+def march(uniforms, textures, width, height, precision=32, pixel_mode=0, coverage_offset=0.0, ref_uv_1080p=0,
+          rows=None, col_begin=0, col_step=1, nthreads=0):
+    """Runs the oracle march over a pixel sample.
+
+    textures: dict with weather (h,w,4), curl (h,w,2|4), low_res (d,h,w,4), hi_res (d,h,w,4), night_sky (opt).
+    rows: (begin, end, step) or None for all rows.  Returns (rgba (n_rows, n_cols, 4), depth (n_rows, n_cols),
+    counters [cloudTest, cloudHiRes, iterations, accumulated]).
+    """
+    lib = load()
+    keep = {k: np.ascontiguousarray(v) for k, v in textures.items() if v is not None}
+    t = OracleTextures(_tex(keep.get("weather")), _tex(keep.get("night_sky")), _tex(keep.get("curl")),
+                       _tex(keep.get("low_res")), _tex(keep.get("hi_res")))
+    rb, re_, rs = rows if rows else (0, height, 1)
+    f = OracleFrame(width, height, pixel_mode, coverage_offset, ref_uv_1080p, rb, re_, rs, col_begin, col_step)
+    n_rows = max(0, (re_ - rb + rs - 1) // rs)
+    n_cols = max(0, (width - col_begin + col_step - 1) // col_step)
+    rgba = np.zeros((n_rows, n_cols, 4), np.float32)
+    depth = np.zeros((n_rows, n_cols), np.float32)
+    cnt = np.zeros(4, np.uint64)
+    fn = lib.oracle_march_f32 if precision == 32 else lib.oracle_march_f64
+    rc = fn(C.addressof(uniforms), C.byref(t), C.byref(f), rgba.ctypes.data, depth.ctypes.data, cnt.ctypes.data,
+            nthreads)
+    if rc:
+        raise RuntimeError("oracle march failed: %d" % rc)
+    return rgba, depth, cnt
+
+
+def tonemap(rgba):
+    """tonemap.frag's Uncharted-2 operator on an (..., 4) float array -> (..., 3)."""
+    a = np.ascontiguousarray(rgba, np.float32)
+    out = np.zeros(a.shape[:-1] + (3,), np.float32)
+    load().oracle_tonemap(a.ctypes.data, a.size // 4, out.ctypes.data)
+    return out

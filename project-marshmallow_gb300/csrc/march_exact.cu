@@ -1,0 +1,13 @@
+// march_exact.cu - the cloud march in reproducible arithmetic.  Built with -fmad=false: no
+// contraction into FMA, IEEE division and square root, mm_math.h elementary functions.  With the
+// software sampler its output equals the FP32 CPU oracle bit for bit.
+#include "march_kernel.cuh"
+
+namespace mm {
+
+int launch_march_exact(const MarchLaunch& p, int sampler, cudaStream_t s) {
+    if (sampler == MM_SAMPLER_SOFTWARE) return march::launch_tiled<true, MM_SAMPLER_SOFTWARE>(p, s);
+    return march::launch_tiled<true, MM_SAMPLER_HARDWARE>(p, s);
+}
+
+}  // namespace mm

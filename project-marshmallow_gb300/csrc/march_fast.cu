@@ -1,0 +1,13 @@
+// march_fast.cu - the cloud march in production arithmetic: FMA contraction, SFU exp2/log2 and
+// rsqrt, texture-unit filtering.
+#include "march_kernel.cuh"
+
+namespace mm {
+
+int launch_march_fast(const MarchLaunch& p, int sampler, int format, cudaStream_t s) {
+    (void)format;
+    if (sampler == MM_SAMPLER_SOFTWARE) return march::launch_tiled<false, MM_SAMPLER_SOFTWARE>(p, s);
+    return march::launch_tiled<false, MM_SAMPLER_HARDWARE>(p, s);
+}
+
+}  // namespace mm

@@ -1,0 +1,88 @@
+// mm_internal.h - library-internal declarations shared by the C ABI and the kernel launchers.
+#ifndef MM_INTERNAL_H_
+#define MM_INTERNAL_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../../include/mm.h"
+
+#if defined(MM_HAVE_CUDA_RUNTIME) || defined(__CUDACC__)
+#include <cuda_runtime.h>
+#endif
+
+namespace mm {
+
+// Records `msg` as the calling thread's last error and returns `code`.
+int fail(int code, const char* fmt, ...);
+// Counts device kernel launches made by the library.
+void count_launch(uint64_t n = 1);
+
+#if defined(MM_HAVE_CUDA_RUNTIME) || defined(__CUDACC__)
+
+// Maps a CUDA error to MM_ERR_CUDA / MM_ERR_OUT_OF_MEMORY with the call site in the message.
+int cuda_fail(cudaError_t e, const char* what);
+
+#define MM_CUDA_TRY(call)                                          \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) return ::mm::cuda_fail(e_, #call); \
+    } while (0)
+
+}  // namespace mm
+
+// Library-owned texture: UNORM8 texels in linear device memory (software sampling, copies) and a
+// hardware-filtered copy in a CUDA array with its texture object.
+struct mm_texture_s {
+    int width = 0, height = 0, depth = 0, channels = 0;
+    int format = MM_FORMAT_UNORM8;   // format of the hardware-filtered copy
+    uint8_t* texels = nullptr;       // device, width*height*depth*channels bytes
+    cudaArray_t array = nullptr;
+    cudaTextureObject_t tex = 0;
+    int device = 0;
+};
+
+struct mm_context_s {
+    int device = 0;
+    unsigned int* d_work = nullptr;  // work-queue counters of the persistent march
+    int num_sms = 0;
+};
+
+namespace mm {
+
+// Device-side view of one texture for the kernels.
+struct TexView {
+    cudaTextureObject_t tex;
+    const uint8_t* texels;
+    int w, h, d, channels;
+};
+
+struct MarchLaunch {
+    mm_uniforms u;
+    TexView weather, night, curl, low, hi;
+    float4* rgba;
+    size_t rgba_pitch;  // bytes
+    float* depth;
+    size_t depth_pitch;  // bytes
+    int width, height;
+    int pixel_mode;
+    int phase;
+    float uv_w, uv_h;
+    float coverage_offset;
+    unsigned long long* counters;
+};
+
+// Kernel launchers (one translation unit per arithmetic mode).
+int launch_march_exact(const MarchLaunch& p, int sampler, cudaStream_t s);
+int launch_march_fast(const MarchLaunch& p, int sampler, int format, cudaStream_t s);
+
+// Noise generators (noise.cu).
+int launch_noise(int kind, uint32_t seed, int w, int h, int d, uint8_t* out, cudaStream_t s);
+int launch_ref_curl(uint8_t* out_rgba, float* scratch_curl, float* scratch_bounds, cudaStream_t s);
+int launch_hash_stage(int which, const void* in, uint32_t seed, size_t n, void* out, cudaStream_t s);
+
+#endif  // CUDA runtime available
+
+}  // namespace mm
+
+#endif  // MM_INTERNAL_H_

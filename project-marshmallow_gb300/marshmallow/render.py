@@ -1,0 +1,125 @@
+"""Textures and frames over CUDA device memory for the library's callers in Python.
+
+Device buffers are torch CUDA tensors (torch is only the allocator and stream provider here); all
+work is done by libmm.so's kernels through the C ABI.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import lib as L
+
+DEFAULT_SIZES = {
+    "low_res": (L.NOISE_LOWRES, 128, 128, 128, 4),
+    "hi_res": (L.NOISE_HIRES, 32, 32, 32, 4),
+    "curl": (L.NOISE_CURL2D, 128, 128, 1, 2),
+    "weather": (L.NOISE_WEATHER, 512, 512, 1, 4),
+}
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        import torch
+        return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    if isinstance(stream, int):
+        return C.c_void_p(stream)
+    return C.c_void_p(stream.cuda_stream)
+
+
+class Textures:
+    """The four seeded cloud textures, generated on the GPU by mm_noise_generate."""
+
+    def __init__(self, seed=0, stream=None, handles=None):
+        lib = L.load()
+        self.handles = {}
+        self.seed = seed
+        if handles is not None:
+            self.handles = dict(handles)
+            return
+        s = _stream_ptr(stream)
+        for name, (kind, w, h, d, _) in DEFAULT_SIZES.items():
+            desc = L.NoiseDesc(kind, seed, w, h, d)
+            hnd = C.c_void_p()
+            L.check(lib.mm_noise_generate(C.byref(desc), C.byref(hnd), s), "mm_noise_generate(%s)" % name)
+            self.handles[name] = hnd
+
+    @classmethod
+    def from_arrays(cls, arrays, stream=None, fmt=L.FORMAT_UNORM8):
+        """Textures from host UNORM8 arrays: 2D (h, w, c) or 3D (d, h, w, c)."""
+        lib = L.load()
+        s = _stream_ptr(stream)
+        handles = {}
+        for name, a in arrays.items():
+            if a is None:
+                continue
+            a = np.ascontiguousarray(a, np.uint8)
+            if a.ndim == 3:
+                d, (h, w, c) = 1, a.shape
+            else:
+                d, h, w, c = a.shape
+            hnd = C.c_void_p()
+            L.check(lib.mm_texture_create(a.ctypes.data, 0, w, h, d, c, fmt, C.byref(hnd), s), "mm_texture_create")
+            handles[name] = hnd
+        return cls(handles=handles)
+
+    def host(self, name):
+        lib = L.load()
+        w, h, d, c, f = (C.c_int() for _ in range(5))
+        hnd = self.handles[name]
+        L.check(lib.mm_texture_info(hnd, C.byref(w), C.byref(h), C.byref(d), C.byref(c), C.byref(f)))
+        shape = (h.value, w.value, c.value) if d.value == 1 else (d.value, h.value, w.value, c.value)
+        out = np.zeros(shape, np.uint8)
+        L.check(lib.mm_texture_copy_to_host(hnd, out.ctypes.data, out.nbytes), "mm_texture_copy_to_host")
+        return out
+
+    def host_all(self):
+        return {k: self.host(k) for k in self.handles}
+
+    def set_density_format(self, fmt, stream=None):
+        lib = L.load()
+        for k in ("low_res", "hi_res"):
+            L.check(lib.mm_texture_set_format(self.handles[k], fmt, _stream_ptr(stream)), "mm_texture_set_format")
+
+    def scene(self):
+        g = self.handles.get
+        return L.SceneTextures(g("weather"), g("night_sky"), g("curl"), g("low_res"), g("hi_res"))
+
+    def close(self):
+        lib = L.load()
+        for h in self.handles.values():
+            lib.mm_texture_destroy(h)
+        self.handles = {}
+
+
+class Renderer:
+    """An mm_context plus the march call on torch-allocated frames."""
+
+    def __init__(self):
+        self.lib = L.load()
+        self.ctx = C.c_void_p()
+        L.check(self.lib.mm_context_create(C.byref(self.ctx)), "mm_context_create")
+
+    @staticmethod
+    def options(pixel_mode=L.PIXELS_FULL, sampler=L.SAMPLER_HARDWARE, math=L.MATH_FAST, density_format=L.FORMAT_UNORM8,
+                coverage_offset=0.0, ref_uv_1080p=0, counters=None):
+        o = L.MarchOptions()
+        L.load().mm_march_options_default(C.byref(o))
+        o.pixel_mode, o.sampler, o.math, o.density_format = pixel_mode, sampler, math, density_format
+        o.coverage_offset, o.ref_uv_1080p = coverage_offset, ref_uv_1080p
+        o.d_counters = counters.data_ptr() if counters is not None else None
+        return o
+
+    def march(self, u, textures, rgba, depth=None, stream=None, **opts):
+        """rgba: (H, W, 4) float32 CUDA tensor; depth: (H, W) float32 CUDA tensor or None."""
+        h, w = rgba.shape[0], rgba.shape[1]
+        img = L.Image(rgba.data_ptr(), rgba.stride(0) * 4, depth.data_ptr() if depth is not None else None,
+                      depth.stride(0) * 4 if depth is not None else 0, w, h)
+        o = self.options(**opts)
+        st = textures.scene() if isinstance(textures, Textures) else textures
+        L.check(self.lib.mm_clouds_march(self.ctx, C.byref(u), C.byref(st), C.byref(img), C.byref(o),
+                                         _stream_ptr(stream)), "mm_clouds_march")
+
+    def close(self):
+        if self.ctx:
+            self.lib.mm_context_destroy(self.ctx)
+            self.ctx = C.c_void_p()

@@ -1,0 +1,70 @@
+"""Regenerates the committed golden fixtures from the reference tree (development machine only).
+
+  curl_fbm_128.rgba   Textures/CurlNoiseFBM.tga decoded to 128x128 RGBA8 (rows top to bottom),
+                      checked equal to the output of the reference's own GenerateCurlNoise
+                      (ImageUtils.cpp compiled by `make -C oracle ref`).
+  ref_hash.txt        hashNoise(x, y, z) of ImageUtils.cpp:25 for a set of lattice points, from the
+                      compiled reference.
+  sky_reference.json  UniformSunObject / UniformSkyObject after SkyManager::rebuildSkyFromNewSun and
+                      setTime (SkyManager.cpp, compiled by `make -C oracle ref`).
+  nubis_stats.json    mean / deviation of the shipped Nubis density textures (the targets of the
+                      seeded generators' output maps).
+
+Usage: python tests/golden/make_golden.py [REFERENCE_ROOT]
+"""
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, "tests"))
+from tga import read_tga  # noqa: E402
+
+
+def main():
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    se = os.path.join(ref, "SkyEngine", "SkyEngine")
+    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", "REF=" + ref], check=True)
+    bins = os.path.join(REPO, "oracle", "_ref")
+
+    shipped = read_tga(os.path.join(se, "Textures", "CurlNoiseFBM.tga"))
+    tmp = os.path.join(bins, "curl_from_reference.tga")
+    subprocess.run([os.path.join(bins, "ref_curlgen"), tmp], check=True)
+    built = read_tga(tmp)
+    assert shipped.shape == (128, 128, 4) and np.array_equal(shipped, built), "reference build != shipped TGA"
+    shipped.tofile(os.path.join(HERE, "curl_fbm_128.rgba"))
+
+    rng = np.random.default_rng(7)
+    pts = [(x, y, z) for x in range(-1, 26, 3) for y in range(-1, 26, 4) for z in range(-1, 26, 5)]
+    pts += [tuple(float(v) for v in rng.uniform(-30, 30, 3).astype(np.float32)) for _ in range(200)]
+    inp = "".join("%.9g %.9g %.9g\n" % p for p in pts)
+    out = subprocess.run([os.path.join(bins, "ref_curlgen"), "--hash"], input=inp, capture_output=True, text=True,
+                         check=True).stdout
+    with open(os.path.join(HERE, "ref_hash.txt"), "w") as f:
+        f.write("# x y z hashNoise(x,y,z) from ImageUtils.cpp:25 (compiled reference)\n" + out)
+
+    triples = [(e, a, t) for e in (0.02, 0.1, 0.2, 0.3, 0.45, 0.6, 0.75, 0.9) for a in (0.25, 0.1, 0.4)
+               for t in (0.0, 7.5)]
+    inp = "".join("%.9g %.9g %.9g\n" % t for t in triples)
+    out = subprocess.run([os.path.join(bins, "ref_sky")], input=inp, capture_output=True, text=True, check=True).stdout
+    with open(os.path.join(HERE, "sky_reference.json"), "w") as f:
+        json.dump(json.loads(out), f, indent=0)
+
+    d3 = os.path.join(se, "Textures", "3DTextures")
+    lo = np.stack([read_tga(os.path.join(d3, "lowResCloudShape", "lowResCloud(%d).tga" % i)) for i in range(128)])
+    hi = np.stack([read_tga(os.path.join(d3, "hiResCloudShape", "hiResClouds (%d).tga" % i)) for i in range(32)])
+    stats = {}
+    for name, a in (("low_res", lo), ("hi_res", hi)):
+        f = a.reshape(-1, 4).astype(np.float64) / 255.0
+        stats[name] = {"mean": f.mean(0).round(4).tolist(), "std": f.std(0).round(4).tolist()}
+    with open(os.path.join(HERE, "nubis_stats.json"), "w") as f:
+        json.dump(stats, f, indent=1)
+    print("fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,184 @@
+"""The CUDA cloud march vs the CPU oracle of compute-clouds.comp.
+
+Gates (colour errors in 1/255 of the reference tonemap, tonemap.frag:10-28):
+  - exact arithmetic + software sampler vs the FP32 oracle: identical output and identical work
+    counters (bit-exact);
+  - production path (FMA, SFU functions, texture-unit filtering) vs the FP64 oracle:
+    RMSE <= 1/255 and max <= 4/255 over 99.9% of pixels (p99.9), depth relative error <= 1e-3 on
+    99.9% of pixels where both are finite.  Pixels where a threshold of the march (density > 0,
+    accumulated density > 0.99, ...) falls the other way take a different path; the share of
+    such pixels is bounded too.
+"""
+import numpy as np
+import pytest
+
+from gpu_util import render, render_counted
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gpu_textures(cuda, mmlib):
+    import marshmallow as mm
+    t = mm.render.Textures(seed=0)
+    yield t
+    t.close()
+
+
+@pytest.fixture(scope="module")
+def host_textures(gpu_textures):
+    return gpu_textures.host_all()
+
+
+@pytest.fixture(scope="module")
+def renderer(cuda, mmlib):
+    import marshmallow as mm
+    r = mm.render.Renderer()
+    yield r
+    r.close()
+
+
+def test_gpu_textures_equal_oracle_textures(host_textures, oracle_textures):
+    for k in oracle_textures:
+        assert np.array_equal(host_textures[k], oracle_textures[k]), k
+
+
+def test_exact_software_bit_exact_256(cuda, orc, renderer, gpu_textures, host_textures):
+    import marshmallow as mm
+    import marshmallow.lib as L
+    u = mm.scene.uniforms(256, 256)
+    rgba, dep, cnt = render_counted(cuda, renderer, u, gpu_textures, 256, 256, sampler=L.SAMPLER_SOFTWARE,
+                                    math=L.MATH_EXACT)
+    ref, rdep, rcnt = orc.march(u, host_textures, 256, 256, precision=32)
+    assert np.array_equal(rgba.view(np.uint32), ref.view(np.uint32))
+    assert np.array_equal(dep.view(np.uint32), rdep.view(np.uint32))
+    assert np.array_equal(cnt, rcnt)
+
+
+@pytest.mark.parametrize("frame", [0, 7, 15])
+def test_exact_software_bit_exact_1080p_rows(cuda, orc, renderer, gpu_textures, host_textures, frame):
+    import marshmallow as mm
+    import marshmallow.lib as L
+    u = mm.scene.sweep_uniforms(frame, 1920, 1080)
+    rgba, dep = render(cuda, renderer, u, gpu_textures, 1920, 1080, sampler=L.SAMPLER_SOFTWARE, math=L.MATH_EXACT)
+    ref, rdep, _ = orc.march(u, host_textures, 1920, 1080, precision=32, rows=(frame, 1080, 24))
+    assert np.array_equal(rgba[frame::24].view(np.uint32), ref.view(np.uint32))
+    assert np.array_equal(dep[frame::24].view(np.uint32), rdep.view(np.uint32))
+
+
+def _gates(e):
+    assert e["nan"] == 0
+    assert e["rmse_255"] <= 1.0, e
+    assert e["p999_255"] <= 4.0, e
+    assert e["frac_over_4"] <= 0.002, e
+    assert e.get("depth_rel_p999", 0.0) <= 1e-3, e
+
+
+@pytest.mark.parametrize("sampler", [0, 1])
+def test_fast_vs_fp64_oracle_256(cuda, orc, renderer, gpu_textures, host_textures, sampler):
+    import marshmallow as mm
+    u = mm.scene.uniforms(256, 256)
+    rgba, dep = render(cuda, renderer, u, gpu_textures, 256, 256, sampler=sampler)
+    ref, rdep, _ = orc.march(u, host_textures, 256, 256, precision=64)
+    e = mm.metrics.frame_errors(rgba, ref, dep, rdep)
+    print("fast sampler=%d vs fp64:" % sampler, e)
+    _gates(e)
+
+
+@pytest.mark.parametrize("frame", [0, 5, 10, 15])
+def test_fast_vs_fp64_oracle_1080p_sweep(cuda, orc, renderer, gpu_textures, host_textures, frame):
+    import marshmallow as mm
+    u = mm.scene.sweep_uniforms(frame, 1920, 1080)
+    rgba, dep = render(cuda, renderer, u, gpu_textures, 1920, 1080)
+    ref, rdep, _ = orc.march(u, host_textures, 1920, 1080, precision=64, rows=(frame % 8, 1080, 8))
+    e = mm.metrics.frame_errors(rgba[frame % 8::8], ref, dep[frame % 8::8], rdep)
+    print("1080p frame %d fast vs fp64:" % frame, e)
+    _gates(e)
+
+
+def test_exact_vs_fp64_oracle_1080p(cuda, orc, renderer, gpu_textures, host_textures):
+    import marshmallow as mm
+    import marshmallow.lib as L
+    u = mm.scene.sweep_uniforms(3, 1920, 1080)
+    rgba, dep = render(cuda, renderer, u, gpu_textures, 1920, 1080, sampler=L.SAMPLER_SOFTWARE, math=L.MATH_EXACT)
+    ref, rdep, _ = orc.march(u, host_textures, 1920, 1080, precision=64, rows=(1, 1080, 8))
+    e = mm.metrics.frame_errors(rgba[1::8], ref, dep[1::8], rdep)
+    print("1080p exact vs fp64:", e)
+    _gates(e)
+
+
+def test_phase16_updates_one_pixel_in_16(cuda, renderer, gpu_textures):
+    import marshmallow as mm
+    import marshmallow.lib as L
+    u = mm.scene.uniforms(200, 120)
+    full, dfull = render(cuda, renderer, u, gpu_textures, 200, 120, sampler=L.SAMPLER_SOFTWARE, math=L.MATH_EXACT)
+    for phase in (0, 6, 15):
+        u.sun.color[3] = float(phase)
+        part, dpart = render(cuda, renderer, u, gpu_textures, 200, 120, pixel_mode=L.PIXELS_PHASE16,
+                             sampler=L.SAMPLER_SOFTWARE, math=L.MATH_EXACT)
+        m = np.zeros((120, 200), bool)
+        m[phase // 4::4, phase % 4::4] = True
+        assert np.array_equal(part[m], full[m]) and np.all(part[~m] == 0)
+
+
+def test_reference_uv_mode(cuda, orc, renderer, gpu_textures, host_textures):
+    # uv = pixel / (1920, 1080) as the shader hard-codes (compute-clouds.comp:283-285, 305).
+    import marshmallow as mm
+    import marshmallow.lib as L
+    u = mm.scene.uniforms(320, 180)
+    rgba, _ = render(cuda, renderer, u, gpu_textures, 320, 180, sampler=L.SAMPLER_SOFTWARE, math=L.MATH_EXACT,
+                     ref_uv_1080p=1)
+    ref, _, _ = orc.march(u, host_textures, 320, 180, precision=32, ref_uv_1080p=1)
+    assert np.array_equal(rgba, ref)
+
+
+def test_coverage_offset_and_sun_sweep(cuda, orc, renderer, gpu_textures, host_textures):
+    import marshmallow as mm
+    import marshmallow.lib as L
+    for el, off in ((5.0, -0.2), (60.0, 0.2), (85.0, 0.0)):
+        u = mm.scene.uniforms(128, 96, sun_elevation=el)
+        rgba, dep = render(cuda, renderer, u, gpu_textures, 128, 96, sampler=L.SAMPLER_SOFTWARE, math=L.MATH_EXACT,
+                           coverage_offset=off)
+        ref, rdep, _ = orc.march(u, host_textures, 128, 96, precision=32, coverage_offset=off)
+        assert np.array_equal(rgba, ref) and np.array_equal(dep, rdep)
+
+
+def test_night_branch(cuda, orc, renderer, gpu_textures, host_textures):
+    import marshmallow as mm
+    import marshmallow.lib as L
+    night = np.random.default_rng(0).integers(0, 256, (90, 160, 4), dtype=np.uint8)
+    nt = mm.render.Textures.from_arrays({"night_sky": night})
+    handles = dict(gpu_textures.handles)
+    handles["night_sky"] = nt.handles["night_sky"]
+    tex = mm.render.Textures(handles=handles)
+    u = mm.scene.uniforms(96, 64, sun_elevation=-12.0)
+    rgba, dep = render(cuda, renderer, u, tex, 96, 64, sampler=L.SAMPLER_SOFTWARE, math=L.MATH_EXACT)
+    h = dict(host_textures)
+    h["night_sky"] = night
+    ref, rdep, _ = orc.march(u, h, 96, 64, precision=32)
+    assert np.array_equal(rgba, ref)
+    nt.close()
+
+
+def test_march_rejects_bad_arguments(cuda, mmlib, renderer, gpu_textures):
+    import ctypes as C
+    import marshmallow as mm
+    import marshmallow.lib as L
+    u = mm.scene.uniforms(64, 64)
+    rgba = cuda.zeros((64, 64, 4), dtype=cuda.float32, device="cuda")
+    st = gpu_textures.scene()
+    o = mm.render.Renderer.options()
+    img = L.Image(rgba.data_ptr(), 8, None, 0, 64, 64)  # pitch too small
+    assert mmlib.mm_clouds_march(renderer.ctx, C.byref(u), C.byref(st), C.byref(img), C.byref(o), None) == 1
+    img = L.Image(rgba.data_ptr(), 64 * 16, None, 0, 64, 64)
+    bad = L.SceneTextures(st.weather, None, None, st.low_res, st.hi_res)
+    assert mmlib.mm_clouds_march(renderer.ctx, C.byref(u), C.byref(bad), C.byref(img), C.byref(o), None) == 1
+    assert b"curl" in mmlib.mm_last_error_string()
+    un = mm.scene.uniforms(64, 64, sun_elevation=-5.0)
+    assert mmlib.mm_clouds_march(renderer.ctx, C.byref(un), C.byref(st), C.byref(img), C.byref(o), None) == 1
+    o.math = 7
+    assert mmlib.mm_clouds_march(renderer.ctx, C.byref(u), C.byref(st), C.byref(img), C.byref(o), None) == 1
+    o = mm.render.Renderer.options(pixel_mode=L.PIXELS_PHASE16)
+    u.sun.color[3] = 16.0
+    assert mmlib.mm_clouds_march(renderer.ctx, C.byref(u), C.byref(st), C.byref(img), C.byref(o), None) == 1
+    cuda.cuda.synchronize()

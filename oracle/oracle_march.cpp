@@ -395,7 +395,11 @@ struct March {
         const T hg = Fn<T>::max(hgPhase(cosTheta, T(0.6)), T(0.7) * hgPhase(cosTheta, T(0.99) - T(0.1)));
         const V3<T> windScale = {T(0.1), T(0.05), T(0)};
 
-        for (T t = inner.t; t < outer.t; t += stepSize) {  // :408-482
+        // :408-482.  The shader's loop ends by t >= outer.t, accumulated density or MAX_STEPS counted
+        // steps; the iteration cap below (never reached by a ray that starts inside the shells) bounds
+        // rays whose uncounted iterations could otherwise run long on degenerate uniforms.
+        int iterations = 0;
+        for (T t = inner.t; t < outer.t && iterations < 8192; t += stepSize, ++iterations) {
             cnt->iterations++;
             V3<T> pos = cameraPos + t * rd;
             V3<T> proj = projectedShellPoint(pos, earthCenter);

@@ -161,6 +161,7 @@ __device__ __forceinline__ F4 sample3d(const TexView& t, V3 p) {
 // ------------------------------------------------------------------------------ shader functions
 
 constexpr float kRadius = 2000000.0f;  // ATMOSPHERE_RADIUS (:56)
+constexpr int kMaxIterations = 8192;    // loop-iteration cap per ray (the CPU oracle uses the same)
 
 template <bool E>
 __device__ __forceinline__ float hgPhase(float cosTheta, float g) {  // :73-77
@@ -394,7 +395,10 @@ __device__ void march_pixel(const MarchLaunch& p, int px, int py, unsigned long 
     const float hg = fmaxf(hgPhase<E>(cosTheta, 0.6f), 0.7f * hgPhase<E>(cosTheta, 0.99f - 0.1f));
     const V3 windScale = {0.1f, 0.05f, 0.0f};
 
-    for (float t = inner.t; t < outer.t; t += stepSize) {  // :408-482
+    // :408-482, with an iteration cap (kMaxIterations) that no ray starting inside the shells reaches;
+    // it bounds the loop for degenerate uniforms.
+    int iterations = 0;
+    for (float t = inner.t; t < outer.t && iterations < kMaxIterations; t += stepSize, ++iterations) {
         ++n_iter;
         V3 pos = cameraPos + t * rd;
         V3 proj = projectedShellPoint<E>(pos, center);

@@ -44,6 +44,9 @@ def parse_args():
     ap.add_argument("--height", type=int, default=2160)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--sampler", choices=["hardware", "software"], default="hardware")
+    ap.add_argument("--math", choices=["fast", "exact"], default="fast")
+    ap.add_argument("--schedule", choices=["persistent", "tiled"], default="tiled")
     return ap.parse_args()
 
 
@@ -210,8 +213,13 @@ def run_ours(args):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     uniforms = [frame_uniforms(k, w, h) for k in range(SWEEP)]
 
+    sampler_mode = L.SAMPLER_HARDWARE if args.sampler == "hardware" else L.SAMPLER_SOFTWARE
+    math_mode = L.MATH_FAST if args.math == "fast" else L.MATH_EXACT
+    schedule = L.SCHEDULE_PERSISTENT if args.schedule == "persistent" else L.SCHEDULE_TILED
+
     def march(k, out_rgba=rgba, out_depth=depth, s=None, counters=None):
-        renderer.march(uniforms[k % SWEEP], textures, out_rgba, out_depth, stream=s, counters=counters)
+        renderer.march(uniforms[k % SWEEP], textures, out_rgba, out_depth, stream=s, counters=counters,
+                       sampler=sampler_mode, math=math_mode, schedule=schedule)
 
     for k in range(args.warmup):
         march(k)
@@ -334,11 +342,12 @@ def run_ours(args):
             "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_frame, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "cloud march %dx%d, plain FP32, hardware-filtered UNORM8 textures, "
-                                   "16-frame sweep" % (w, h),
+            "config": {"workload": "cloud march %dx%d, plain FP32, %s-filtered UNORM8 textures, "
+                                   "16-frame sweep" % (w, h, args.sampler),
                        "width": w, "height": h, "frames_cycled": SWEEP, "textures": "seed 0, generated on GPU",
                        "l2": "flushed between frames (256 MB memset outside the timed events)",
-                       "variant": "plain", "math": "fast", "sampler": "hardware"},
+                       "variant": "plain", "math": args.math, "sampler": args.sampler,
+                       "schedule": args.schedule},
             "roofline": {"bound": "tex", "achieved": round(achieved_gfetch, 2), "peak": round(peak_eff, 1),
                          "unit": "Gfetch/s",
                          "frac": round(tex_time_frac, 4), "traffic": traffic,

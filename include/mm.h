@@ -225,6 +225,16 @@ typedef enum mm_math_mode {
                           when combined with MM_SAMPLER_SOFTWARE */
 } mm_math_mode;
 
+typedef enum mm_schedule {
+    MM_SCHEDULE_TILED = 0,      /* one thread marches one pixel start to end (the shader's own loop
+                                   nest), 8x4 pixel tiles per warp, the six sun-cone taps of a sample
+                                   fetched together */
+    MM_SCHEDULE_PERSISTENT = 1  /* persistent warps; each iteration evaluates one cloudTest per lane
+                                   (a march step or a sun-cone tap); finished lanes take the next ray
+                                   of their warp's 8x4 pixel tile (ballot compaction).  Full SIMT
+                                   lanes, but a warp's texture requests scatter over more texels */
+} mm_schedule;
+
 typedef struct mm_march_options {
     int pixel_mode;        /* mm_pixel_mode */
     int sampler;           /* mm_sampler_mode */
@@ -235,10 +245,11 @@ typedef struct mm_march_options {
                               (compute-clouds.comp:283-285,305); 0: uv = pixel / (width,height) */
     uint64_t* d_counters;  /* optional device uint64[4]: cloudTest calls, cloudHiRes calls,
                               loop iterations, accumulated samples (atomically added) */
+    int schedule;          /* mm_schedule */
 } mm_march_options;
 
 /* Fills `o` with the defaults: full frame, hardware sampler, fast math, UNORM8, offset 0,
- * uv = pixel/(width,height), no counters. */
+ * uv = pixel/(width,height), no counters, tiled schedule. */
 int mm_march_options_default(mm_march_options* o);
 
 typedef struct mm_context_s* mm_context;

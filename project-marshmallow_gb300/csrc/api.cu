@@ -344,6 +344,8 @@ int mm_clouds_march(mm_context ctx, const mm_uniforms* u, const mm_scene_texture
     if (o.sampler != MM_SAMPLER_HARDWARE && o.sampler != MM_SAMPLER_SOFTWARE)
         return fail(MM_ERR_INVALID_ARGUMENT, "march: bad sampler %d", o.sampler);
     if (o.math != MM_MATH_FAST && o.math != MM_MATH_EXACT) return fail(MM_ERR_INVALID_ARGUMENT, "march: bad math %d", o.math);
+    if (o.schedule != MM_SCHEDULE_PERSISTENT && o.schedule != MM_SCHEDULE_TILED)
+        return fail(MM_ERR_INVALID_ARGUMENT, "march: bad schedule %d", o.schedule);
     if (o.density_format < MM_FORMAT_UNORM8 || o.density_format > MM_FORMAT_BF16)
         return fail(MM_ERR_INVALID_ARGUMENT, "march: bad density_format %d", o.density_format);
     if (!(o.coverage_offset == o.coverage_offset) || o.coverage_offset < -1.0f || o.coverage_offset > 1.0f)
@@ -401,8 +403,8 @@ int mm_clouds_march(mm_context ctx, const mm_uniforms* u, const mm_scene_texture
     p.coverage_offset = o.coverage_offset;
     p.counters = reinterpret_cast<unsigned long long*>(o.d_counters);
     cudaStream_t s = (cudaStream_t)stream;
-    if (o.math == MM_MATH_EXACT) return mm::launch_march_exact(p, o.sampler, s);
-    return mm::launch_march_fast(p, o.sampler, o.density_format, s);
+    if (o.math == MM_MATH_EXACT) return mm::launch_march_exact(p, o.sampler, o.schedule, ctx->d_work, ctx->num_sms, s);
+    return mm::launch_march_fast(p, o.sampler, o.density_format, o.schedule, ctx->d_work, ctx->num_sms, s);
 }
 
 }  // extern "C"

@@ -5,9 +5,15 @@
 
 namespace mm {
 
-int launch_march_exact(const MarchLaunch& p, int sampler, cudaStream_t s) {
-    if (sampler == MM_SAMPLER_SOFTWARE) return march::launch_tiled<true, MM_SAMPLER_SOFTWARE>(p, s);
-    return march::launch_tiled<true, MM_SAMPLER_HARDWARE>(p, s);
+int launch_march_exact(const MarchLaunch& p, int sampler, int schedule, unsigned int* work, int num_sms,
+                       cudaStream_t s) {
+    if (schedule == MM_SCHEDULE_TILED) {
+        if (sampler == MM_SAMPLER_SOFTWARE) return march::launch_tiled<true, MM_SAMPLER_SOFTWARE>(p, s);
+        return march::launch_tiled<true, MM_SAMPLER_HARDWARE>(p, s);
+    }
+    if (sampler == MM_SAMPLER_SOFTWARE)
+        return march::launch_persistent<true, MM_SAMPLER_SOFTWARE>(p, work, num_sms, s);
+    return march::launch_persistent<true, MM_SAMPLER_HARDWARE>(p, work, num_sms, s);
 }
 
 }  // namespace mm

@@ -4,10 +4,16 @@
 
 namespace mm {
 
-int launch_march_fast(const MarchLaunch& p, int sampler, int format, cudaStream_t s) {
+int launch_march_fast(const MarchLaunch& p, int sampler, int format, int schedule, unsigned int* work, int num_sms,
+                      cudaStream_t s) {
     (void)format;
-    if (sampler == MM_SAMPLER_SOFTWARE) return march::launch_tiled<false, MM_SAMPLER_SOFTWARE>(p, s);
-    return march::launch_tiled<false, MM_SAMPLER_HARDWARE>(p, s);
+    if (schedule == MM_SCHEDULE_TILED) {
+        if (sampler == MM_SAMPLER_SOFTWARE) return march::launch_tiled<false, MM_SAMPLER_SOFTWARE>(p, s);
+        return march::launch_tiled<false, MM_SAMPLER_HARDWARE>(p, s);
+    }
+    if (sampler == MM_SAMPLER_SOFTWARE)
+        return march::launch_persistent<false, MM_SAMPLER_SOFTWARE>(p, work, num_sms, s);
+    return march::launch_persistent<false, MM_SAMPLER_HARDWARE>(p, work, num_sms, s);
 }
 
 }  // namespace mm

@@ -1,9 +1,11 @@
 // march_kernel.cuh - the cloud raymarch of compute-clouds.comp:288-500 as CUDA device code.
 //
 // One thread marches one pixel-ray.  The code is a template over
-//   kExact   - true: IEEE +,-,*,/,sqrt and the mm_math.h elementary functions, for a translation
-//              unit compiled with -fmad=false (bit-identical to the FP32 CPU oracle when the
-//              software sampler is used); false: FMA contraction and the SFU approximations.
+//   kExact   - true: the shader's arithmetic as written, IEEE +,-,*,/,sqrt and the mm_math.h
+//              elementary functions, for a translation unit compiled with -fmad=false
+//              (bit-identical to the FP32 CPU oracle when the software sampler is used);
+//              false: the same quantities by cheaper, algebraically equal forms (below) with FMA
+//              contraction and the SFU approximations.
 //   kSampler - MM_SAMPLER_SOFTWARE (float-weight trilinear from the UNORM8 texels, the sampler
 //              definition of the oracle) or MM_SAMPLER_HARDWARE (texture objects: LINEAR, WRAP,
 //              normalized coordinates; 8-bit fixed-point filter weights).
@@ -17,6 +19,23 @@
 
 #include "mm_internal.h"
 #include "mm_math.h"
+
+// Build knobs (defaults measured best on GB300 at 3840x2160): warps per block of the tiled kernel
+// (4 or 8) and the minimum resident blocks per SM requested from the register allocator for it
+// (4 warps x 9 blocks: 56 registers, 36 warps per SM); the same for the persistent kernel; and
+// the speculative curl fetch of the tiled march (off: it costs more occupancy than it hides).
+#ifndef MM_TILED_WARPS
+#define MM_TILED_WARPS 4
+#endif
+#ifndef MM_MARCH_MIN_BLOCKS
+#define MM_MARCH_MIN_BLOCKS (MM_TILED_WARPS == 4 ? 9 : 4)
+#endif
+#ifndef MM_PERSISTENT_MIN_BLOCKS
+#define MM_PERSISTENT_MIN_BLOCKS 3
+#endif
+#ifndef MM_SPEC_CURL
+#define MM_SPEC_CURL 0
+#endif
 
 namespace mm {
 namespace march {
@@ -222,44 +241,235 @@ __device__ __forceinline__ float cloudLayerDensity(float rh, float type) {  // :
     return mixf(d1, d2, type);
 }
 
-struct Scene {
-    V3 cam;
-    V3 center;
-    V3 wind;
-    float time;
-    float thickness;
-    float coverage_offset;
+// ------------------------------------------------------------------------------ per-launch constants
+
+struct Frame {
+    V3 cam, center, wind, sunDir;
+    float time, sunY, thickness, coverage_offset;
+    // fast-path forms: 20 * wind and 20 * (0.1, 0.05, 0)
+    V3 wind20, wscale20;
+};
+
+template <bool E>
+__device__ __forceinline__ Frame make_frame(const MarchLaunch& p) {
+    const mm_uniforms& u = p.u;
+    Frame f;
+    f.cam = ld3(u.camera.camera_position);
+    f.center = f.cam;
+    f.center.y = -kRadius * 0.5f * 0.995f;  // :357-358
+    f.wind = ld3(u.sky.wind);
+    f.time = u.sky.wind[3];  // :289
+    f.sunDir = normalize<E>(ld3(u.sun.direction_basis + 4));  // :324
+    f.sunY = u.sun.direction[1];
+    f.thickness = 0.5f * kRadius * 0.02f;  // :360
+    f.coverage_offset = p.coverage_offset;
+    f.wind20 = 20.0f * f.wind;
+    f.wscale20 = {2.0f, 1.0f, 0.0f};
+    return f;
+}
+
+// Cone offsets mat3(directionBasis) * v (:392-401), computed once per block into shared memory
+// by threads 0..5 (the caller synchronizes).
+__device__ __forceinline__ void cone_offsets(const mm_uniforms& u, V3* out) {
+    const int i = threadIdx.x;
+    if (i >= 6) return;
+    const float* b = u.sun.direction_basis;
+    float x, y, z;
+    switch (i) {
+        case 0: x = 0.0f; y = 0.6f; z = 0.0f; break;
+        case 1: x = 0.0f; y = 0.5f; z = 0.05f; break;
+        case 2: x = 0.1f; y = 0.75f; z = 0.0f; break;
+        case 3: x = 0.2f; y = 2.5f; z = 0.3f; break;
+        case 4: x = 0.0f; y = 6.0f; z = 0.0f; break;
+        default: x = -0.1f; y = 1.0f; z = -0.2f; break;
+    }
+    out[i] = {(b[0] * x + b[4] * y) + b[8] * z, (b[1] * x + b[5] * y) + b[9] * z, (b[2] * x + b[6] * y) + b[10] * z};
+}
+
+// ------------------------------------------------------------------------------ sample evaluation
+//
+// A density sample at point `pos` (a march step or a cone tap): relative height of pos, the wind
+// offset at that height (:414, :445) and the wind-displaced point sp that cloudTest/cloudHiRes
+// read (:421, :436, :447, :450).
+//
+// Fast-path identities used when kExact is false (the exact path keeps the shader's forms):
+//  - getRelativeHeight(pos, getProjectedShellPoint(pos, c), T) (:180-188): pos - proj is
+//    d * (1 - R/|d|) with d = pos - c and R = 0.5 * ATMOSPHERE_RADIUS, so its length is
+//    | |d| - R |: one square root instead of a normalize, a subtraction and a length.
+//  - the weather coordinate 0.000009 * (proj(sp).xz - camera.xz) (:236): the earth centre shares
+//    the camera's x and z (:357-358), so proj.xz - cam.xz = R * d2.xz / |d2| with d2 = sp - c,
+//    i.e. 9 * d2.xz * rsqrt(|d2|^2).
+//  - remap/remapClamped with constant bounds folded into one multiply-add; the three layer
+//    profiles of cloudLayerDensity (:193-204) as 25 h (0.9 - h), 10 h (0.7 - h), 100 h (0.3 - h).
+//  - cloudTest's low-res fetch is skipped where the layer density is exactly zero (the product
+//    layer * remapClamped(...) is zero whatever the texel holds, :240, :243).
+
+struct Geo {
+    V3 sp;     // wind-displaced sample point
+    V3 d2;     // sp - earth centre (fast path)
+    float rh;  // relative height of the undisplaced point
+};
+
+template <bool E>
+__device__ __forceinline__ Geo geo_at(const Frame& f, V3 pos) {
+    Geo g;
+    if (E) {
+        V3 proj = projectedShellPoint<E>(pos, f.center);
+        g.rh = relativeHeight<E>(pos, proj, f.thickness);
+        const V3 windScale = {0.1f, 0.05f, 0.0f};
+        V3 wo = (20.0f * (f.wind + g.rh * windScale)) * (f.time + g.rh * 200.0f);
+        g.sp = pos + wo;
+        g.d2 = g.sp - f.center;
+    } else {
+        const V3 d = pos - f.center;
+        const float len = sqrtf(dot(d, d));
+        g.rh = __saturatef(fabsf(len - 0.5f * kRadius) * (1.0f / 20000.0f));
+        const float k = f.time + g.rh * 200.0f;
+        V3 wo = {(f.wind20.x + g.rh * f.wscale20.x) * k, (f.wind20.y + g.rh * f.wscale20.y) * k, f.wind20.z * k};
+        g.sp = pos + wo;
+        g.d2 = d + wo;
+    }
+    return g;
+}
+
+__device__ __forceinline__ float layer_fast(float h, float type) {
+    const float cumulus = fmaxf(0.0f, 25.0f * h * (0.9f - h));
+    const float strato = fmaxf(0.0f, 10.0f * h * (0.7f - h));
+    const float stratus = fmaxf(0.0f, 100.0f * h * (0.3f - h));
+    const float d1 = stratus + (strato - stratus) * __saturatef(type * 2.0f);
+    const float d2 = strato + (cumulus - strato) * __saturatef(type * 2.0f - 1.0f);
+    return d1 + (d2 - d1) * type;
+}
+
+// cloudTest (:231-253) in two halves so independent fetches can be in flight together: the
+// weather and low-res fetches of one sample (and of several cone taps) are issued before any of
+// their results is used.
+struct TestFetch {
+    float cov, type;  // weather.r, weather.b
+    F4 dn;            // low-res density noise
 };
 
 template <bool E, int S>
-__device__ __forceinline__ float cloudTest(const MarchLaunch& p, const Scene& sc, V3 pos, float rh,
-                                           unsigned long long& n_test) {  // :231-253
+__device__ __forceinline__ TestFetch test_fetch(const MarchLaunch& p, const Frame& f, const Geo& g) {
+    TestFetch r;
+    F4 info;
+    if (E) {
+        V3 proj = projectedShellPoint<E>(g.sp, f.center);
+        info = sample2d<E, S>(p.weather, 0.000009f * (proj.x - f.cam.x), 0.000009f * (proj.z - f.cam.z));
+    } else {
+        const float rr = rsqrtf(dot(g.d2, g.d2));
+        info = sample2d<E, S>(p.weather, 9.0f * rr * g.d2.x, 9.0f * rr * g.d2.z);
+    }
+    r.cov = info.x;
+    r.type = info.z;
+    r.dn = sample3d<E, S>(p.low, 0.00002f * g.sp);
+    return r;
+}
+
+template <bool E>
+__device__ __forceinline__ float test_finish(const Frame& f, const Geo& g, const TestFetch& c,
+                                             unsigned long long& n_test) {
     ++n_test;
-    V3 proj = projectedShellPoint<E>(pos, sc.center);
-    F4 info = sample2d<E, S>(p.weather, 0.000009f * (proj.x - sc.cam.x), 0.000009f * (proj.z - sc.cam.z));
-    float layer = cloudLayerDensity<E>(rh, info.z);
-    F4 dn = sample3d<E, S>(p.low, 0.00002f * pos);
-    float density = layer * remapClamped<E>(dn.x, 0.3f, 1.0f, 0.0f, 1.0f);
-    if (density < 0.0001f) return 0.0f;
-    // heightBiasCoverage(relativeHeight, min(0.85, weather.r)) with its arguments swapped as in :245
-    float h = fminf(0.85f, info.x + sc.coverage_offset);
-    float coverage = M<E>::pow(rh, clampf(remap<E>(h, 0.7f, 0.8f, 1.0f, 0.8f), 0.8f, 1.0f));
-    float erosion = 0.625f * dn.y + 0.25f * dn.z + 0.125f * dn.w;
-    erosion = remapClamped<E>(erosion, coverage, 1.0f, 0.0f, 1.0f);
-    return remapClamped<E>(density, erosion, 1.0f, 0.0f, 1.0f);
+    if (E) {
+        float layer = cloudLayerDensity<E>(g.rh, c.type);
+        float density = layer * remapClamped<E>(c.dn.x, 0.3f, 1.0f, 0.0f, 1.0f);
+        if (density < 0.0001f) return 0.0f;
+        // heightBiasCoverage(relativeHeight, min(0.85, weather.r)) with its arguments swapped (:245)
+        float h = fminf(0.85f, c.cov + f.coverage_offset);
+        float coverage = M<E>::pow(g.rh, clampf(remap<E>(h, 0.7f, 0.8f, 1.0f, 0.8f), 0.8f, 1.0f));
+        float erosion = 0.625f * c.dn.y + 0.25f * c.dn.z + 0.125f * c.dn.w;
+        erosion = remapClamped<E>(erosion, coverage, 1.0f, 0.0f, 1.0f);
+        return remapClamped<E>(density, erosion, 1.0f, 0.0f, 1.0f);
+    } else {
+        const float layer = layer_fast(g.rh, c.type);
+        const float density = layer * __saturatef(c.dn.x * (1.0f / 0.7f) - (0.3f / 0.7f));
+        if (!(density >= 0.0001f)) return 0.0f;
+        const float h = fminf(0.85f, c.cov + f.coverage_offset);
+        const float e = clampf(1.0f - (h - 0.7f) * 2.0f, 0.8f, 1.0f);
+        const float coverage = e == 1.0f ? g.rh : exp2f(e * __log2f(g.rh));
+        const float ero = 0.625f * c.dn.y + 0.25f * c.dn.z + 0.125f * c.dn.w;
+        const float erosion = __saturatef((ero - coverage) * __frcp_rn(1.0f - coverage));
+        return __saturatef((density - erosion) * __frcp_rn(1.0f - erosion));
+    }
 }
 
 template <bool E, int S>
-__device__ __forceinline__ float cloudHiRes(const MarchLaunch& p, V3 pos, float curlStrength, float orig, float rh,
-                                            unsigned long long& n_hires) {  // :214-228
+__device__ __forceinline__ float cloud_test(const MarchLaunch& p, const Frame& f, const Geo& g,
+                                            unsigned long long& n_test) {
+    return test_finish<E>(f, g, test_fetch<E, S>(p, f, g), n_test);
+}
+
+// cloudHiRes (:214-228) in three stages: curl fetch, displaced hi-res fetch, erosion.
+template <bool E, int S>
+__device__ __forceinline__ V3 hires_point(const MarchLaunch& p, const Geo& g, float curlStrength) {
+    const V3 pos = g.sp;
+    const F4 c = sample2d<E, S>(p.curl, 0.0001f * pos.x, 0.0001f * pos.z);
+    if (E) {
+        V3 curl = {2.0f * c.x - 1.0f, 2.0f * c.y - 1.0f, 2.0f * c.z - 1.0f};
+        return pos + 1.9f * curlStrength * curl;
+    } else {
+        const float k = 1.9f * curlStrength;
+        return {pos.x + k * (2.0f * c.x - 1.0f), pos.y + k * (2.0f * c.y - 1.0f), pos.z + k * (2.0f * c.z - 1.0f)};
+    }
+}
+
+template <bool E, int S>
+__device__ __forceinline__ F4 hires_fetch(const MarchLaunch& p, V3 q) {
+    return sample3d<E, S>(p.hi, 0.0004f * q);
+}
+
+template <bool E>
+__device__ __forceinline__ float hires_finish(const F4& dn, float rh, float orig, unsigned long long& n_hires) {
     ++n_hires;
-    F4 c = sample2d<E, S>(p.curl, 0.0001f * pos.x, 0.0001f * pos.z);
-    V3 curl = {2.0f * c.x - 1.0f, 2.0f * c.y - 1.0f, 2.0f * c.z - 1.0f};
-    pos = pos + 1.9f * curlStrength * curl;
-    F4 dn = sample3d<E, S>(p.hi, 0.0004f * pos);
-    float erosion = 0.625f * dn.x + 0.25f * dn.y + 0.125f * dn.z;
-    erosion = mixf(erosion, 1.0f - erosion, clampf(rh * 10.0f, 0.0f, 1.0f));
-    return remapClamped<E>(orig, 1.0f * erosion, 1.0f, 0.0f, 1.0f);
+    if (E) {
+        float erosion = 0.625f * dn.x + 0.25f * dn.y + 0.125f * dn.z;
+        erosion = mixf(erosion, 1.0f - erosion, clampf(rh * 10.0f, 0.0f, 1.0f));
+        return remapClamped<E>(orig, 1.0f * erosion, 1.0f, 0.0f, 1.0f);
+    } else {
+        float e = 0.625f * dn.x + 0.25f * dn.y + 0.125f * dn.z;
+        e = e + (1.0f - 2.0f * e) * __saturatef(rh * 10.0f);
+        return __saturatef((orig - e) * __frcp_rn(1.0f - e));
+    }
+}
+
+template <bool E, int S>
+__device__ __forceinline__ float cloud_hires(const MarchLaunch& p, const Geo& g, float curlStrength, float orig,
+                                             unsigned long long& n_hires) {
+    return hires_finish<E>(hires_fetch<E, S>(p, hires_point<E, S>(p, g, curlStrength)), g.rh, orig, n_hires);
+}
+
+#ifndef MM_CONE_GROUP
+#define MM_CONE_GROUP 1  // cone taps whose fetches are issued together (1, 2, 3 or 6)
+#endif
+
+// Sun-cone taps i0 .. i0+G-1 of one sample (:441-453): their fetches are issued together; the
+// densities are added to densityAlongLight in tap order.
+template <bool E, int S, int G>
+__device__ __forceinline__ float cone_taps(const MarchLaunch& p, const Frame& f, const V3* cone, int i0, V3 pos,
+                                           float stepSize, float dal, unsigned long long& n_test,
+                                           unsigned long long& n_hires) {
+    Geo g[G];
+    TestFetch c[G];
+#pragma unroll
+    for (int j = 0; j < G; ++j) {
+        g[j] = geo_at<E>(f, pos + 3.0f * stepSize * cone[i0 + j]);
+        c[j] = test_fetch<E, S>(p, f, g[j]);
+    }
+    float d[G];
+#pragma unroll
+    for (int j = 0; j < G; ++j) d[j] = test_finish<E>(f, g[j], c[j], n_test);
+    V3 q[G];
+#pragma unroll
+    for (int j = 0; j < G; ++j)
+        if (d[j] > 0.0f) q[j] = hires_point<E, S>(p, g[j], stepSize);
+    F4 hv[G];
+#pragma unroll
+    for (int j = 0; j < G; ++j)
+        if (d[j] > 0.0f) hv[j] = hires_fetch<E, S>(p, q[j]);
+#pragma unroll
+    for (int j = 0; j < G; ++j)
+        if (d[j] > 0.0f) dal += hires_finish<E>(hv[j], g[j].rh, d[j], n_hires);
+    return dal;
 }
 
 struct Isect {
@@ -287,31 +497,33 @@ __device__ __forceinline__ Isect raySphere(V3 ro, V3 rd, V3 c, float w) {  // :1
     return is;
 }
 
-// The whole of main() (:288-500) for pixel (px, py).  Writes colour and depth.
+// Per-ray set-up of main() (:292-407): ray direction, sky colour, horizon kill, shell
+// intersections, night sky, phase function.
+struct Ray {
+    V3 rd, bg;
+    float alpha;    // finalColor.a before the cloud term
+    float t0, t1;   // inner / outer shell distances
+    float cosTheta, hg;
+    bool killed;    // rd.y < 0: stored as is (:351-354)
+};
+
 template <bool E, int S>
-__device__ void march_pixel(const MarchLaunch& p, int px, int py, unsigned long long* cnt) {
+__device__ __forceinline__ Ray ray_setup(const MarchLaunch& p, const Frame& f, int px, int py) {
     const mm_uniforms& u = p.u;
-    unsigned long long n_test = 0, n_hires = 0, n_iter = 0, n_acc = 0;
-    Scene sc;
-    sc.time = u.sky.wind[3];
-    sc.wind = ld3(u.sky.wind);
-    sc.coverage_offset = p.coverage_offset;
+    Ray r;
     const float* view = u.camera.view;
     float uvx = M<E>::div((float)px, p.uv_w), uvy = M<E>::div((float)py, p.uv_h);
     float spx = uvx * 2.0f - 1.0f, spy = uvy * 2.0f - 1.0f;
     V3 camLook = {view[2], view[6], view[10]};
     V3 camRight = {view[0], view[4], view[8]};
     V3 camUp = {view[1], view[5], view[9]};
-    const V3 cameraPos = ld3(u.camera.camera_position);
-    sc.cam = cameraPos;
-    V3 refPoint = cameraPos - camLook;
+    V3 refPoint = f.cam - camLook;
     const float cpx = u.camera.camera_params[0], cpy = u.camera.camera_params[1];
     V3 q = refPoint + cpx * spx * cpy * camRight - spy * cpy * camUp;
-    V3 rd = normalize<E>(q - cameraPos);
+    r.rd = normalize<E>(q - f.cam);
+    const V3 rd = r.rd;
 
-    V3 sunDir = normalize<E>(ld3(u.sun.direction_basis + 4));
-    const float sunY = u.sun.direction[1];
-    float dotToSun = fmaxf(0.0f, dot(sunDir, rd));
+    float dotToSun = fmaxf(0.0f, dot(f.sunDir, rd));
     float skyAmbient = dotToSun * 0.18f;
     skyAmbient *= skyAmbient * skyAmbient;
     const float SUN_ANGULAR_COS = 0.999956676946448443553574619906976478926848692873900859324f;
@@ -321,91 +533,138 @@ __device__ void march_pixel(const MarchLaunch& p, int px, int py, unsigned long 
     dotToSun *= dotToSun * dotToSun * dotToSun;
     dotToSun *= dotToSun * dotToSun * dotToSun;
     dotToSun *= dotToSun * dotToSun;
-    if (sunY < 0.0f) dotToSun *= dotToSun * dotToSun * dotToSun * dotToSun * dotToSun * dotToSun;
+    if (f.sunY < 0.0f) dotToSun *= dotToSun * dotToSun * dotToSun * dotToSun * dotToSun * dotToSun;
     sunDisk = fmaxf(sunDisk, dotToSun);
     sunDisk = fmaxf(0.0f, sunDisk);
 
-    float4 fc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    V3 bg = {0.0f, 0.0f, 0.0f};
-    if (sunY >= 0.0f) {
-        bg = atmosphereColor<E>(u, rd, sunDir);
-        fc.w = fmaxf(skyAmbient, sunDisk);
-        fc.x = bg.x;
-        fc.y = bg.y;
-        fc.z = bg.z;
+    r.alpha = 0.0f;
+    r.bg = {0.0f, 0.0f, 0.0f};
+    if (f.sunY >= 0.0f) {
+        r.bg = atmosphereColor<E>(u, rd, f.sunDir);
+        r.alpha = fmaxf(skyAmbient, sunDisk);
     }
-    float4* out = reinterpret_cast<float4*>(reinterpret_cast<char*>(p.rgba) + (size_t)py * p.rgba_pitch) + px;
-    float* dout = p.depth ? reinterpret_cast<float*>(reinterpret_cast<char*>(p.depth) + (size_t)py * p.depth_pitch) + px
-                          : nullptr;
-    if (dot(rd, V3{0.0f, 1.0f, 0.0f}) < 0.0f) {  // :351-354
-        *out = fc;
-        if (dout) *dout = CUDART_INF_F;
-        return;
-    }
+    r.killed = dot(rd, V3{0.0f, 1.0f, 0.0f}) < 0.0f;
+    r.t0 = r.t1 = 0.0f;
+    r.cosTheta = 0.0f;
+    r.hg = 0.0f;
+    if (r.killed) return r;
 
-    V3 center = cameraPos;
-    center.y = -kRadius * 0.5f * 0.995f;
-    sc.center = center;
-    const float thickness = 0.5f * kRadius * 0.02f;
-    sc.thickness = thickness;
-    Isect inner = raySphere<E>(cameraPos, rd, center, kRadius);
-    Isect outer = raySphere<E>(cameraPos, rd, center, kRadius * 1.02f);
+    r.t0 = raySphere<E>(f.cam, rd, f.center, kRadius).t;
+    r.t1 = raySphere<E>(f.cam, rd, f.center, kRadius * 1.02f).t;
 
-    if (sunY < 0.0f) {  // :365-384
+    if (f.sunY < 0.0f) {  // :365-384
         const float nrm = M<E>::rsqrt(2.0f);
         V3 ax = {1.0f * nrm, 0.0f * nrm, 1.0f * nrm};
-        float ang = sunY * 0.5f;
+        float ang = f.sunY * 0.5f;
         float c = M<E>::cos(ang), s = M<E>::sin(ang);
         V3 c0 = {c + ax.x * ax.x * (1.0f - c), ax.y * ax.x * (1.0f - c) + ax.z * s, ax.z * ax.x * (1.0f - c) - ax.y * s};
         V3 c1 = {ax.x * ax.y * (1.0f - c) - ax.z * s, c + ax.y * ax.y * (1.0f - c), ax.z * ax.y * (1.0f - c) + ax.x * s};
         V3 c2 = {ax.x * ax.z * (1.0f - c) + ax.y * s, ax.y * ax.z * (1.0f - c) - ax.x * s, c + ax.z * ax.z * (1.0f - c)};
         V3 rrd = {(c0.x * rd.x + c1.x * rd.y) + c2.x * rd.z, (c0.y * rd.x + c1.y * rd.y) + c2.y * rd.z,
                   (c0.z * rd.x + c1.z * rd.y) + c2.z * rd.z};
-        V3 rro = {(c0.x * cameraPos.x + c1.x * cameraPos.y) + c2.x * cameraPos.z,
-                  (c0.y * cameraPos.x + c1.y * cameraPos.y) + c2.y * cameraPos.z,
-                  (c0.z * cameraPos.x + c1.z * cameraPos.y) + c2.z * cameraPos.z};
-        V3 point = outer.t * rrd + rro;
-        V3 pp = projectedShellPoint<E>(point, center);
-        F4 ns = sample2d<E, S>(p.night, 0.00002f * (pp.x - cameraPos.x) + 0.35f, 0.00002f * (pp.z - cameraPos.z) + 0.35f);
-        bg = {ns.x, ns.y, ns.z};
+        const V3 cp = f.cam;
+        V3 rro = {(c0.x * cp.x + c1.x * cp.y) + c2.x * cp.z, (c0.y * cp.x + c1.y * cp.y) + c2.y * cp.z,
+                  (c0.z * cp.x + c1.z * cp.y) + c2.z * cp.z};
+        V3 point = r.t1 * rrd + rro;
+        V3 pp = projectedShellPoint<E>(point, f.center);
+        F4 ns = sample2d<E, S>(p.night, 0.00002f * (pp.x - cp.x) + 0.35f, 0.00002f * (pp.z - cp.z) + 0.35f);
+        V3 bg = {ns.x, ns.y, ns.z};
         bg = bg * (V3{M<E>::sqrt(bg.x), M<E>::sqrt(bg.y), M<E>::sqrt(bg.z)} * 0.75f);
         bg = {M<E>::pow(bg.x, 2.2f), M<E>::pow(bg.y, 2.2f), M<E>::pow(bg.z, 2.2f)};
         bg = bg * 10.0f;
         float falloff = M<E>::pow(rd.y, 6.0f);
         bg = bg * falloff;
         bg = mix3(V3{0.3f, 0.6f, 4.0f} * 0.05f, bg, M<E>::pow(rd.y, 0.03125f));
-        bg = bg + sunDisk;
-        fc.w = sunDisk;
+        r.bg = bg + sunDisk;
+        r.alpha = sunDisk;
     }
+    r.cosTheta = dot(rd, f.sunDir);  // :386
+    r.hg = fmaxf(hgPhase<E>(r.cosTheta, 0.6f), 0.7f * hgPhase<E>(r.cosTheta, 0.99f - 0.1f));  // :407
+    return r;
+}
 
-    const float cosTheta = dot(rd, sunDir);
+// Beer's law, in-scatter and the front-to-back blend of one accumulated sample (:455-464).
+template <bool E>
+__device__ __forceinline__ float shade(float trans, float accum, float dal, float lo, float rh, float cosTheta,
+                                       float hg) {
+    float beers = M<E>::exp(-dal);
+    float beersMod = fmaxf(beers, 0.7f * M<E>::exp(-0.25f * dal));
+    beers = mixf(beers, beersMod, -cosTheta * 0.5f + 0.5f);
+    float inScatter = 0.09f + M<E>::pow(lo, remapClamped<E>(rh, 0.3f, 0.85f, 0.5f, 2.0f));
+    inScatter *= M<E>::pow(remapClamped<E>(rh, 0.07f, 0.34f, 0.1f, 1.0f), 0.8f);
+    return mixf(trans, inScatter * hg * beers, 1.0f - accum);
+}
+
+// End of main() (:484-499): horizon fade, cloud colour, composite.
+template <bool E>
+__device__ __forceinline__ float4 composite(const mm_uniforms& u, const Frame& f, V3 rd, V3 bg, float alpha,
+                                            float accum, float transmittance) {
+    accum *= smoothstep<E>(0.0f, 1.0f, fminf(1.0f, remap<E>(rd.y, 0.0f, 0.1f, 0.0f, 1.0f)));
+    accum = fminf(accum, 0.999f);
+    const V3 sunColor = ld3(u.sun.color);
+    const float I = u.sun.intensity;
+    const float et = M<E>::exp(-transmittance);
+    const float a = I * fmaxf(0.0f, transmittance);
+    V3 cloud;
+    if (f.sunY >= 0.0f) {
+        cloud = sunColor * (V3{a, a, a} + (0.08f * bg) * et);
+    } else {
+        V3 night = V3{0.3f, 0.6f, 4.0f} * 0.05f * M<E>::pow(rd.y, 0.03125f);
+        cloud = sunColor * (V3{a, a, a} + (0.08f * night) * et);
+    }
+    V3 rgb = mix3(bg, cloud, accum);
+    return make_float4(rgb.x, rgb.y, rgb.z, alpha * fmaxf(1.0f - accum, 0.0f));
+}
+
+__device__ __forceinline__ void store_pixel(const MarchLaunch& p, int px, int py, float4 c, float depth) {
+    float4* out = reinterpret_cast<float4*>(reinterpret_cast<char*>(p.rgba) + (size_t)py * p.rgba_pitch) + px;
+    *out = c;
+    if (p.depth) *(reinterpret_cast<float*>(reinterpret_cast<char*>(p.depth) + (size_t)py * p.depth_pitch) + px) = depth;
+}
+
+struct Work {
+    unsigned long long test = 0, hires = 0, iter = 0, acc = 0;
+};
+
+__device__ __forceinline__ void flush_work(unsigned long long* cnt, const Work& w) {
+    if (!cnt) return;
+    atomicAdd(cnt + 0, w.test);
+    atomicAdd(cnt + 1, w.hires);
+    atomicAdd(cnt + 2, w.iter);
+    atomicAdd(cnt + 3, w.acc);
+}
+
+// ------------------------------------------------------------------------------ tiled kernel
+
+// The whole of main() (:288-500) for pixel (px, py) in one thread, the shader's own loop structure.
+template <bool E, int S>
+__device__ void march_pixel(const MarchLaunch& p, const Frame& f, const V3* cone, int px, int py, Work& w) {
+    const Ray r = ray_setup<E, S>(p, f, px, py);
+    if (r.killed) {
+        store_pixel(p, px, py, make_float4(r.bg.x, r.bg.y, r.bg.z, r.alpha), CUDART_INF_F);
+        return;
+    }
+    const V3 rd = r.rd;
     float accum = 0.0f, transmittance = 1.0f;
-    float stepSize = 0.05f * thickness;
-    const V3 b0 = ld3(u.sun.direction_basis + 0), b1 = ld3(u.sun.direction_basis + 4),
-             b2 = ld3(u.sun.direction_basis + 8);
-    // mat3(directionBasis) * v for the six cone offsets (:392-401)
-    auto bm = [&](float x, float y, float z) -> V3 {
-        return {(b0.x * x + b1.x * y) + b2.x * z, (b0.y * x + b1.y * y) + b2.y * z, (b0.z * x + b1.z * y) + b2.z * z};
-    };
-    const V3 samples[6] = {bm(0.0f, 0.6f, 0.0f), bm(0.0f, 0.5f, 0.05f), bm(0.1f, 0.75f, 0.0f),
-                           bm(0.2f, 2.5f, 0.3f), bm(0.0f, 6.0f, 0.0f),  bm(-0.1f, 1.0f, -0.2f)};
+    float stepSize = 0.05f * f.thickness;  // :390
     bool noHits = true;
     int misses = 0, steps = 0;
     float firstT = CUDART_INF_F;
-    const float hg = fmaxf(hgPhase<E>(cosTheta, 0.6f), 0.7f * hgPhase<E>(cosTheta, 0.99f - 0.1f));
-    const V3 windScale = {0.1f, 0.05f, 0.0f};
-
-    // :408-482, with an iteration cap (kMaxIterations) that no ray starting inside the shells reaches;
-    // it bounds the loop for degenerate uniforms.
+    // :408-482, with an iteration cap (kMaxIterations) that no ray starting inside the shells
+    // reaches; it bounds the loop for degenerate uniforms.
     int iterations = 0;
-    for (float t = inner.t; t < outer.t && iterations < kMaxIterations; t += stepSize, ++iterations) {
-        ++n_iter;
-        V3 pos = cameraPos + t * rd;
-        V3 proj = projectedShellPoint<E>(pos, center);
-        float rh = relativeHeight<E>(pos, proj, thickness);
-        V3 windOffset = (20.0f * (sc.wind + rh * windScale)) * (sc.time + rh * 200.0f);
-        float density = cloudTest<E, S>(p, sc, pos + windOffset, rh, n_test);
-        float loDensity = density;
+    for (float t = r.t0; t < r.t1 && iterations < kMaxIterations; t += stepSize, ++iterations) {
+        ++w.iter;
+        const V3 pos = f.cam + t * rd;
+        const Geo g = geo_at<E>(f, pos);
+#if MM_SPEC_CURL
+        // Once the ray marches in small steps, a sample that finds density goes on to cloudHiRes;
+        // its curl fetch is issued with the cloudTest fetches so the two latencies overlap.
+        V3 qh;
+        if (!noHits) qh = hires_point<E, S>(p, g, stepSize);
+#endif
+        float density = cloud_test<E, S>(p, f, g, w.test);
+        const float loDensity = density;
         if (density > 0.0f) {
             misses = 0;
             if (noHits) {
@@ -414,28 +673,19 @@ __device__ void march_pixel(const MarchLaunch& p, int px, int py, unsigned long 
                 noHits = false;
                 continue;
             }
-            density = cloudHiRes<E, S>(p, pos + windOffset, stepSize, density, rh, n_hires);
+#if MM_SPEC_CURL
+            density = hires_finish<E>(hires_fetch<E, S>(p, qh), g.rh, density, w.hires);
+#else
+            density = cloud_hires<E, S>(p, g, stepSize, density, w.hires);
+#endif
             if (density < 0.0001f) continue;
             float densityAlongLight = 0.0f;
 #pragma unroll 1
-            for (int i = 0; i < 6; i++) {
-                V3 lsPos = pos + 3.0f * stepSize * samples[i];
-                V3 lsProj = projectedShellPoint<E>(lsPos, center);
-                float lsHeight = relativeHeight<E>(lsPos, lsProj, thickness);
-                windOffset = (20.0f * (sc.wind + lsHeight * windScale)) * (sc.time + lsHeight * 200.0f);
-                float lsDensity = cloudTest<E, S>(p, sc, lsPos + windOffset, lsHeight, n_test);
-                if (lsDensity > 0.0f) {
-                    lsDensity = cloudHiRes<E, S>(p, lsPos + windOffset, stepSize, lsDensity, lsHeight, n_hires);
-                    densityAlongLight += lsDensity;
-                }
-            }
-            float beers = M<E>::exp(-densityAlongLight);
-            float beersMod = fmaxf(beers, 0.7f * M<E>::exp(-0.25f * densityAlongLight));
-            beers = mixf(beers, beersMod, -cosTheta * 0.5f + 0.5f);
-            float inScatter = 0.09f + M<E>::pow(loDensity, remapClamped<E>(rh, 0.3f, 0.85f, 0.5f, 2.0f));
-            inScatter *= M<E>::pow(remapClamped<E>(rh, 0.07f, 0.34f, 0.1f, 1.0f), 0.8f);
-            transmittance = mixf(transmittance, inScatter * hg * beers, 1.0f - accum);
-            ++n_acc;
+            for (int i = 0; i < 6; i += MM_CONE_GROUP)
+                densityAlongLight = cone_taps<E, S, MM_CONE_GROUP>(p, f, cone, i, pos, stepSize, densityAlongLight,
+                                                                   w.test, w.hires);
+            transmittance = shade<E>(transmittance, accum, densityAlongLight, loDensity, g.rh, r.cosTheta, r.hg);
+            ++w.acc;
             if (firstT == CUDART_INF_F) firstT = t;
             accum += density;
         } else if (!noHits) {
@@ -451,42 +701,22 @@ __device__ void march_pixel(const MarchLaunch& p, int px, int py, unsigned long 
         }
         if (++steps > 100) break;
     }
-
-    accum *= smoothstep<E>(0.0f, 1.0f, fminf(1.0f, remap<E>(rd.y, 0.0f, 0.1f, 0.0f, 1.0f)));
-    accum = fminf(accum, 0.999f);
-    const V3 sunColor = ld3(u.sun.color);
-    const float I = u.sun.intensity;
-    const float et = M<E>::exp(-transmittance);
-    const float a = I * fmaxf(0.0f, transmittance);
-    V3 cloud;
-    if (sunY >= 0.0f) {
-        cloud = sunColor * (V3{a, a, a} + (0.08f * bg) * et);
-    } else {
-        V3 night = V3{0.3f, 0.6f, 4.0f} * 0.05f * M<E>::pow(rd.y, 0.03125f);
-        cloud = sunColor * (V3{a, a, a} + (0.08f * night) * et);
-    }
-    V3 rgb = mix3(bg, cloud, accum);
-    fc.x = rgb.x;
-    fc.y = rgb.y;
-    fc.z = rgb.z;
-    fc.w *= fmaxf(1.0f - accum, 0.0f);
-    *out = fc;
-    if (dout) *dout = firstT;
-    if (cnt) {
-        atomicAdd(cnt + 0, n_test);
-        atomicAdd(cnt + 1, n_hires);
-        atomicAdd(cnt + 2, n_iter);
-        atomicAdd(cnt + 3, n_acc);
-    }
+    store_pixel(p, px, py, composite<E>(p.u, f, r.rd, r.bg, r.alpha, accum, transmittance), firstT);
 }
 
-// Ray-tile order: a block covers a 32x8 pixel tile; each warp an 8x4 sub-tile, so one warp's 32
-// rays are a compact footprint in the density textures.
+// Ray-tile order: each warp marches an 8x4 pixel sub-tile, so one warp's 32 rays are a compact
+// footprint in the density textures; a block of MM_TILED_WARPS warps covers 32x8 (8 warps) or
+// 16x8 (4 warps) pixels.
+constexpr int kBlockTileW = MM_TILED_WARPS == 8 ? 32 : 16;
+constexpr int kBlockTileH = 8;
 template <bool E, int S>
-__global__ void __launch_bounds__(256) march_tiled_kernel(MarchLaunch p) {
+__global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_MARCH_MIN_BLOCKS) march_tiled_kernel(MarchLaunch p) {
+    __shared__ V3 s_cone[6];
+    cone_offsets(p.u, s_cone);
+    __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int tx = blockIdx.x * 32 + (warp & 3) * 8 + (lane & 7);
-    const int ty = blockIdx.y * 8 + (warp >> 2) * 4 + (lane >> 3);
+    const int tx = blockIdx.x * kBlockTileW + (warp % (kBlockTileW / 8)) * 8 + (lane & 7);
+    const int ty = blockIdx.y * kBlockTileH + (warp / (kBlockTileW / 8)) * 4 + (lane >> 3);
     int px, py;
     if (p.pixel_mode == MM_PIXELS_PHASE16) {  // :292-298 (thread grid covers ceil(W/4) x ceil(H/4))
         px = tx * 4 + (p.phase % 4);
@@ -496,7 +726,10 @@ __global__ void __launch_bounds__(256) march_tiled_kernel(MarchLaunch p) {
         py = ty;
     }
     if (px >= p.width || py >= p.height) return;  // :301 with the runtime image size
-    march_pixel<E, S>(p, px, py, p.counters);
+    const Frame f = make_frame<E>(p);
+    Work w;
+    march_pixel<E, S>(p, f, s_cone, px, py, w);
+    flush_work(p.counters, w);
 }
 
 template <bool E, int S>
@@ -506,10 +739,226 @@ int launch_tiled(const MarchLaunch& p, cudaStream_t s) {
         gw = (p.width + 3) / 4;
         gh = (p.height + 3) / 4;
     }
-    dim3 grid((gw + 31) / 32, (gh + 7) / 8);
-    march_tiled_kernel<E, S><<<grid, 256, 0, s>>>(p);
+    dim3 grid((gw + kBlockTileW - 1) / kBlockTileW, (gh + kBlockTileH - 1) / kBlockTileH);
+    march_tiled_kernel<E, S><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "march_tiled_kernel launch");
+    count_launch();
+    return MM_OK;
+}
+
+// ------------------------------------------------------------------------------ persistent kernel
+//
+// Each warp keeps 32 rays in flight.  One iteration of the loop below evaluates, for every lane,
+// exactly one cloudTest (either the lane's next march step or its next sun-cone tap) and, where
+// the shader would, one cloudHiRes; a lane whose ray ends stores it and takes the next ray of its
+// warp's 8x4 pixel tile (ballot over the idle lanes), and a warp that has used up its tile takes
+// the next tile from a global counter.  Every ray executes the same sequence of operations as in
+// march_pixel; only the interleaving of rays on the SIMT lanes changes.
+
+constexpr int kTileW = 8, kTileH = 4;
+constexpr int kWarps = 8;  // warps per block of the persistent kernel
+
+
+// A ray whose set-up is done, waiting in its warp's queue for an idle lane.
+struct Pending {
+    float rdx, rdy, rdz, bgx, bgy, bgz, alpha, t0, t1, cosTheta, hg;
+    int pix;  // py * 65536 + px
+};
+
+template <bool E, int S>
+__global__ void __launch_bounds__(256, MM_PERSISTENT_MIN_BLOCKS) march_persistent_kernel(MarchLaunch p, unsigned int* tile_counter, int tiles_x,
+                                                               int n_tiles, int grid_w, int grid_h) {
+    __shared__ V3 s_cone[6];
+    __shared__ Pending s_queue[kWarps][32];
+    cone_offsets(p.u, s_cone);
+    __syncthreads();
+    const unsigned lane_id = threadIdx.x & 31;
+    Pending* queue = s_queue[threadIdx.x >> 5];
+    const Frame f = make_frame<E>(p);
+    Work w;
+    // Lane state of one ray (the locals of main() that live across loop iterations).
+    int px = -1, py = 0;  // px < 0: no ray
+    V3 rd, bg, pos;
+    float alpha = 0.f, t = 0.f, t1 = 0.f, stepSize = 0.f, accum = 0.f, trans = 0.f, firstT = 0.f, cosTheta = 0.f,
+          hg = 0.f, rh = 0.f, lo = 0.f, dens = 0.f, dal = 0.f;
+    int misses = 0, steps = 0, iterations = 0, cone = -1;
+    bool noHits = true;
+    int queued = 0;          // warp-uniform: rays waiting in the queue (taken from the top)
+    bool exhausted = false;  // warp-uniform: no tiles left
+
+    while (true) {
+        unsigned need = __ballot_sync(0xffffffffu, px < 0);
+        // ---- the warp sets up the 32 rays of its next tile together, one per lane; rays that
+        // leave the frame or point below the horizon (:351-354) are stored here and not queued.
+        if (need && queued == 0 && !exhausted) {
+            int tv = 0;
+            if (lane_id == 0) tv = (int)atomicAdd(tile_counter, 1u);
+            const int tile = __shfl_sync(0xffffffffu, tv, 0);
+            if (tile >= n_tiles) {
+                exhausted = true;
+            } else {
+                const int gx = (tile % tiles_x) * kTileW + (lane_id % kTileW);
+                const int gy = (tile / tiles_x) * kTileH + (lane_id / kTileW);
+                int qx = gx, qy = gy;
+                if (p.pixel_mode == MM_PIXELS_PHASE16) {
+                    qx = gx * 4 + (p.phase % 4);
+                    qy = gy * 4 + (p.phase / 4);
+                }
+                bool live = false;
+                Ray r;
+                if (gx < grid_w && gy < grid_h && qx < p.width && qy < p.height) {
+                    r = ray_setup<E, S>(p, f, qx, qy);
+                    if (r.killed)
+                        store_pixel(p, qx, qy, make_float4(r.bg.x, r.bg.y, r.bg.z, r.alpha), CUDART_INF_F);
+                    else
+                        live = true;
+                }
+                const unsigned lm = __ballot_sync(0xffffffffu, live);
+                if (live) {
+                    Pending& q = queue[__popc(lm & ((1u << lane_id) - 1u))];
+                    q.rdx = r.rd.x; q.rdy = r.rd.y; q.rdz = r.rd.z;
+                    q.bgx = r.bg.x; q.bgy = r.bg.y; q.bgz = r.bg.z;
+                    q.alpha = r.alpha; q.t0 = r.t0; q.t1 = r.t1; q.cosTheta = r.cosTheta; q.hg = r.hg;
+                    q.pix = qy * 65536 + qx;
+                }
+                queued = __popc(lm);
+                __syncwarp();
+            }
+        }
+        // ---- idle lanes take queued rays (ballot rank among the idle lanes)
+        if (need && queued > 0) {
+            const int rank = __popc(need & ((1u << lane_id) - 1u));
+            const int take = min(__popc(need), queued);
+            if (((need >> lane_id) & 1u) && rank < take) {
+                const Pending& q = queue[queued - 1 - rank];
+                px = q.pix & 65535;
+                py = q.pix >> 16;
+                rd = {q.rdx, q.rdy, q.rdz};
+                bg = {q.bgx, q.bgy, q.bgz};
+                alpha = q.alpha;
+                t = q.t0;
+                t1 = q.t1;
+                cosTheta = q.cosTheta;
+                hg = q.hg;
+                stepSize = 0.05f * f.thickness;  // :390
+                accum = 0.0f;
+                trans = 1.0f;
+                firstT = CUDART_INF_F;
+                misses = steps = iterations = 0;
+                noHits = true;
+                cone = -1;
+            }
+            queued -= take;
+            __syncwarp();
+        }
+        const unsigned active = __ballot_sync(0xffffffffu, px >= 0);
+        if (active == 0) {
+            if (exhausted) break;
+            continue;  // every ray of the last tile was stored during set-up
+        }
+        if (px >= 0) {
+            // ---- the loop condition of :408 for a lane about to take a march step
+            bool done = cone < 0 && !(t < t1 && iterations < kMaxIterations);
+            if (!done) {
+                if (cone < 0) {
+                    ++w.iter;
+                    pos = f.cam + t * rd;
+                }
+                // march step: the point itself; cone tap i: pos + 3 stepSize samples[i] (:442)
+                const V3 q = cone < 0 ? pos : pos + 3.0f * stepSize * s_cone[cone];
+                const Geo g = geo_at<E>(f, q);
+                if (cone < 0) rh = g.rh;
+                const float d = cloud_test<E, S>(p, f, g, w.test);
+                float h = 0.0f;
+                if (d > 0.0f && (cone >= 0 || !noHits)) h = cloud_hires<E, S>(p, g, stepSize, d, w.hires);
+
+                bool advance = false, post = false;
+                if (cone < 0) {
+                    lo = d;
+                    if (d > 0.0f) {
+                        misses = 0;
+                        if (noHits) {  // :428-434
+                            t -= stepSize;
+                            stepSize *= 0.3f;
+                            noHits = false;
+                            advance = true;
+                        } else if (h < 0.0001f) {  // :437
+                            advance = true;
+                        } else {
+                            dens = h;
+                            dal = 0.0f;
+                            cone = 0;
+                        }
+                    } else {
+                        if (!noHits) {  // :468-474
+                            misses++;
+                            if (misses >= 10) {
+                                noHits = true;
+                                stepSize = M<E>::div(stepSize, 0.3f);
+                            }
+                        }
+                        post = true;
+                    }
+                } else {
+                    if (d > 0.0f) dal += h;  // :449-452
+                    if (++cone == 6) {       // :456-466
+                        trans = shade<E>(trans, accum, dal, lo, rh, cosTheta, hg);
+                        ++w.acc;
+                        if (firstT == CUDART_INF_F) firstT = t;
+                        accum += dens;
+                        cone = -1;
+                        post = true;
+                    }
+                }
+                if (post) {  // :476-481
+                    if (accum > 0.99f) {
+                        accum = 1.0f;
+                        done = true;
+                    } else if (++steps > 100) {
+                        done = true;
+                    } else {
+                        advance = true;
+                    }
+                }
+                if (advance) {  // the for-loop increment
+                    t += stepSize;
+                    ++iterations;
+                }
+            }
+            if (done) {
+                store_pixel(p, px, py, composite<E>(p.u, f, rd, bg, alpha, accum, trans), firstT);
+                px = -1;
+            }
+        }
+    }
+    flush_work(p.counters, w);
+}
+
+template <bool E, int S>
+int launch_persistent(const MarchLaunch& p, unsigned int* d_counter, int num_sms, cudaStream_t s) {
+    int gw = p.width, gh = p.height;
+    if (p.pixel_mode == MM_PIXELS_PHASE16) {
+        gw = (p.width + 3) / 4;
+        gh = (p.height + 3) / 4;
+    }
+    const int tiles_x = (gw + kTileW - 1) / kTileW, tiles_y = (gh + kTileH - 1) / kTileH;
+    const int n_tiles = tiles_x * tiles_y;
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_persistent_kernel<E, S>, 256, 0) !=
+                cudaSuccess ||
+            per_sm <= 0)
+            per_sm = 1;
+    }
+    int blocks = num_sms * per_sm;
+    if (blocks * kWarps > n_tiles) blocks = (n_tiles + kWarps - 1) / kWarps;
+    if (blocks < 1) blocks = 1;
+    cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess) return cuda_fail(e, "work counter reset");
+    march_persistent_kernel<E, S><<<blocks, 256, 0, s>>>(p, d_counter, tiles_x, n_tiles, gw, gh);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "march_persistent_kernel launch");
     count_launch();
     return MM_OK;
 }

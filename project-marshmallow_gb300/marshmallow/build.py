@@ -34,10 +34,15 @@ def nvcc():
     raise RuntimeError("nvcc not found")
 
 
+def _extra_flags():
+    """Extra nvcc flags from the environment (MM_NVCC_FLAGS), e.g. -DMM_MARCH_MIN_BLOCKS=3."""
+    return os.environ.get("MM_NVCC_FLAGS", "").split()
+
+
 def _cmd_for(unit, obj):
     src = os.path.join(CSRC, unit)
     if unit.endswith(".cu"):
-        flags = list(NVCC_COMMON)
+        flags = list(NVCC_COMMON) + _extra_flags()
         if unit in EXACT_UNITS:
             flags += ["-fmad=false"]
         return [nvcc()] + flags + ["-c", src, "-o", obj]
@@ -52,7 +57,7 @@ def _digest():
             h.update(name.encode() + b"\0" + f.read())
     with open(os.path.join(REPO, "include", "mm.h"), "rb") as f:
         h.update(f.read())
-    h.update(" ".join(NVCC_COMMON + sorted(EXACT_UNITS)).encode())
+    h.update(" ".join(NVCC_COMMON + sorted(EXACT_UNITS) + _extra_flags()).encode())
     h.update(os.uname().machine.encode())
     return h.hexdigest()
 

@@ -22,6 +22,7 @@ FORMAT_UNORM8, FORMAT_FP16, FORMAT_BF16 = range(3)
 PIXELS_FULL, PIXELS_PHASE16 = range(2)
 SAMPLER_HARDWARE, SAMPLER_SOFTWARE = range(2)
 MATH_FAST, MATH_EXACT = range(2)
+SCHEDULE_TILED, SCHEDULE_PERSISTENT = range(2)
 
 F16 = C.c_float * 16
 F4 = C.c_float * 4
@@ -73,7 +74,7 @@ class Image(C.Structure):
 class MarchOptions(C.Structure):
     _fields_ = [("pixel_mode", C.c_int), ("sampler", C.c_int), ("math", C.c_int),
                 ("density_format", C.c_int), ("coverage_offset", C.c_float), ("ref_uv_1080p", C.c_int),
-                ("d_counters", C.c_void_p)]
+                ("d_counters", C.c_void_p), ("schedule", C.c_int)]
 
 
 # Every function include/mm.h declares, with its ctypes signature.

@@ -38,5 +38,7 @@ def frame_errors(rgba, ref_rgba, depth=None, ref_depth=None):
         rel = np.abs(x[both] - y[both]) / np.maximum(np.abs(y[both]), 1e-30)
         out["depth_rel_max"] = float(rel.max()) if rel.size else 0.0
         out["depth_rel_p999"] = float(np.percentile(rel, 99.9)) if rel.size else 0.0
+        out["depth_rel_median"] = float(np.median(rel)) if rel.size else 0.0
+        out["depth_frac_over_1e3"] = float(np.mean(rel > 1e-3)) if rel.size else 0.0
         out["depth_finite_mismatch"] = float(np.mean(np.isfinite(x) != np.isfinite(y)))
     return out

@@ -86,6 +86,7 @@ SIGNATURES = {
     "mm_noise_generate": (C.c_int, [C.POINTER(NoiseDesc), C.POINTER(C.c_void_p), C.c_void_p]),
     "mm_noise_texel_bytes": (C.c_int, [C.POINTER(NoiseDesc), C.POINTER(C.c_size_t)]),
     "mm_noise_fill": (C.c_int, [C.POINTER(NoiseDesc), C.c_void_p, C.c_size_t, C.c_void_p]),
+    "mm_noise_fill_ref_curl_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_size_t, C.c_void_p]),
     "mm_noise_hash3": (C.c_int, [C.c_void_p, C.c_uint32, C.c_size_t, C.c_void_p, C.c_void_p]),
     "mm_ref_curl_hash": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]),
     "mm_texture_create": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,

@@ -47,6 +47,7 @@ def parse_args():
     ap.add_argument("--sampler", choices=["hardware", "software"], default="hardware")
     ap.add_argument("--math", choices=["fast", "exact"], default="fast")
     ap.add_argument("--schedule", choices=["persistent", "tiled"], default="tiled")
+    ap.add_argument("--density", choices=["unorm8", "fp16"], default="unorm8")
     return ap.parse_args()
 
 
@@ -207,6 +208,9 @@ def run_ours(args):
     sptr = C.c_void_p(stream.cuda_stream)
 
     textures = mm.render.Textures(seed=0)
+    density_format = L.FORMAT_FP16 if args.density == "fp16" else L.FORMAT_UNORM8
+    if density_format != L.FORMAT_UNORM8:
+        textures.set_density_format(density_format)
     renderer = mm.render.Renderer()
     rgba = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
     depth = torch.empty((h, w), dtype=torch.float32, device="cuda")
@@ -219,7 +223,7 @@ def run_ours(args):
 
     def march(k, out_rgba=rgba, out_depth=depth, s=None, counters=None):
         renderer.march(uniforms[k % SWEEP], textures, out_rgba, out_depth, stream=s, counters=counters,
-                       sampler=sampler_mode, math=math_mode, schedule=schedule)
+                       sampler=sampler_mode, math=math_mode, schedule=schedule, density_format=density_format)
 
     for k in range(args.warmup):
         march(k)
@@ -265,6 +269,8 @@ def run_ours(args):
 
     # On-chip peaks measured now on this GPU (MEASURED_PEAKS.json holds HBM and bf16 only).
     pk = (C.c_double * 3)()
+    if density_format != L.FORMAT_UNORM8:
+        textures.set_density_format(L.FORMAT_UNORM8)
     L.check(lib.mm_measure_peaks(textures.handles["low_res"], textures.handles["weather"], pk, sptr),
             "mm_measure_peaks")
     peak3d, peak2d, peak_fp32 = pk[0], pk[1], pk[2]
@@ -342,11 +348,11 @@ def run_ours(args):
             "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_frame, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "cloud march %dx%d, plain FP32, %s-filtered UNORM8 textures, "
-                                   "16-frame sweep" % (w, h, args.sampler),
+            "config": {"workload": "cloud march %dx%d, plain FP32, %s-filtered %s density textures, "
+                                   "16-frame sweep" % (w, h, args.sampler, args.density.upper()),
                        "width": w, "height": h, "frames_cycled": SWEEP, "textures": "seed 0, generated on GPU",
                        "l2": "flushed between frames (256 MB memset outside the timed events)",
-                       "variant": "plain", "math": args.math, "sampler": args.sampler,
+                       "variant": "plain", "math": args.math, "sampler": args.sampler, "density": args.density,
                        "schedule": args.schedule},
             "roofline": {"bound": "tex", "achieved": round(achieved_gfetch, 2), "peak": round(peak_eff, 1),
                          "unit": "Gfetch/s",

@@ -322,7 +322,8 @@ __device__ __forceinline__ Geo geo_at(const Frame& f, V3 pos) {
         g.d2 = g.sp - f.center;
     } else {
         const V3 d = pos - f.center;
-        const float len = sqrtf(dot(d, d));
+        const float dd = dot(d, d);
+        const float len = dd * rsqrtf(dd);
         g.rh = __saturatef(fabsf(len - 0.5f * kRadius) * (1.0f / 20000.0f));
         const float k = f.time + g.rh * 200.0f;
         V3 wo = {(f.wind20.x + g.rh * f.wscale20.x) * k, (f.wind20.y + g.rh * f.wscale20.y) * k, f.wind20.z * k};
@@ -388,8 +389,8 @@ __device__ __forceinline__ float test_finish(const Frame& f, const Geo& g, const
         const float e = clampf(1.0f - (h - 0.7f) * 2.0f, 0.8f, 1.0f);
         const float coverage = e == 1.0f ? g.rh : exp2f(e * __log2f(g.rh));
         const float ero = 0.625f * c.dn.y + 0.25f * c.dn.z + 0.125f * c.dn.w;
-        const float erosion = __saturatef((ero - coverage) * __frcp_rn(1.0f - coverage));
-        return __saturatef((density - erosion) * __frcp_rn(1.0f - erosion));
+        const float erosion = __saturatef((ero - coverage) * __fdividef(1.0f, 1.0f - coverage));
+        return __saturatef((density - erosion) * __fdividef(1.0f, 1.0f - erosion));
     }
 }
 
@@ -428,7 +429,7 @@ __device__ __forceinline__ float hires_finish(const F4& dn, float rh, float orig
     } else {
         float e = 0.625f * dn.x + 0.25f * dn.y + 0.125f * dn.z;
         e = e + (1.0f - 2.0f * e) * __saturatef(rh * 10.0f);
-        return __saturatef((orig - e) * __frcp_rn(1.0f - e));
+        return __saturatef((orig - e) * __fdividef(1.0f, 1.0f - e));
     }
 }
 
@@ -709,7 +710,7 @@ __device__ void march_pixel(const MarchLaunch& p, const Frame& f, const V3* cone
 // 16x8 (4 warps) pixels.
 constexpr int kBlockTileW = MM_TILED_WARPS == 8 ? 32 : 16;
 constexpr int kBlockTileH = 8;
-template <bool E, int S>
+template <bool E, int S, bool C>
 __global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_MARCH_MIN_BLOCKS) march_tiled_kernel(MarchLaunch p) {
     __shared__ V3 s_cone[6];
     cone_offsets(p.u, s_cone);
@@ -727,9 +728,9 @@ __global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_MARCH_MIN_BLOCKS) marc
     }
     if (px >= p.width || py >= p.height) return;  // :301 with the runtime image size
     const Frame f = make_frame<E>(p);
-    Work w;
+    Work w;  // work counts; dead code unless C (counters requested)
     march_pixel<E, S>(p, f, s_cone, px, py, w);
-    flush_work(p.counters, w);
+    if (C) flush_work(p.counters, w);
 }
 
 template <bool E, int S>
@@ -740,7 +741,10 @@ int launch_tiled(const MarchLaunch& p, cudaStream_t s) {
         gh = (p.height + 3) / 4;
     }
     dim3 grid((gw + kBlockTileW - 1) / kBlockTileW, (gh + kBlockTileH - 1) / kBlockTileH);
-    march_tiled_kernel<E, S><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
+    if (p.counters)
+        march_tiled_kernel<E, S, true><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
+    else
+        march_tiled_kernel<E, S, false><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "march_tiled_kernel launch");
     count_launch();
@@ -766,7 +770,7 @@ struct Pending {
     int pix;  // py * 65536 + px
 };
 
-template <bool E, int S>
+template <bool E, int S, bool C>
 __global__ void __launch_bounds__(256, MM_PERSISTENT_MIN_BLOCKS) march_persistent_kernel(MarchLaunch p, unsigned int* tile_counter, int tiles_x,
                                                                int n_tiles, int grid_w, int grid_h) {
     __shared__ V3 s_cone[6];
@@ -932,7 +936,7 @@ __global__ void __launch_bounds__(256, MM_PERSISTENT_MIN_BLOCKS) march_persisten
             }
         }
     }
-    flush_work(p.counters, w);
+    if (C) flush_work(p.counters, w);
 }
 
 template <bool E, int S>
@@ -946,7 +950,7 @@ int launch_persistent(const MarchLaunch& p, unsigned int* d_counter, int num_sms
     const int n_tiles = tiles_x * tiles_y;
     static int per_sm = 0;
     if (per_sm == 0) {
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_persistent_kernel<E, S>, 256, 0) !=
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_persistent_kernel<E, S, false>, 256, 0) !=
                 cudaSuccess ||
             per_sm <= 0)
             per_sm = 1;
@@ -956,7 +960,10 @@ int launch_persistent(const MarchLaunch& p, unsigned int* d_counter, int num_sms
     if (blocks < 1) blocks = 1;
     cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned int), s);
     if (e != cudaSuccess) return cuda_fail(e, "work counter reset");
-    march_persistent_kernel<E, S><<<blocks, 256, 0, s>>>(p, d_counter, tiles_x, n_tiles, gw, gh);
+    if (p.counters)
+        march_persistent_kernel<E, S, true><<<blocks, 256, 0, s>>>(p, d_counter, tiles_x, n_tiles, gw, gh);
+    else
+        march_persistent_kernel<E, S, false><<<blocks, 256, 0, s>>>(p, d_counter, tiles_x, n_tiles, gw, gh);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "march_persistent_kernel launch");
     count_launch();

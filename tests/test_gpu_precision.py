@@ -1,0 +1,59 @@
+"""Precision sweep: 3840x2160 frames over sun elevation {5, 30, 60, 85} deg x coverage offset
+{-0.2, 0, +0.2}, UNORM8 and FP16 density textures, production arithmetic, against the FP64 oracle on
+every 8th row and column.  Gates: UNORM8 RMSE <= 1/255 and p99.9 <= 4/255; FP16 RMSE <= 2/255
+(the mixed-precision gate) with at most 0.5% of pixels above 4/255.  FP16 is less accurate than
+UNORM8 here: the texels themselves are k/255 rounded to 11 bits, and the texture unit filters them at
+reduced precision.  Prints the table of errors (colour in 1/255 of the reference tonemap, depth
+relative)."""
+import numpy as np
+import pytest
+
+from gpu_util import render
+
+pytestmark = pytest.mark.gpu
+
+W, H, STEP = 3840, 2160, 8
+
+
+@pytest.fixture(scope="module")
+def setup(cuda, mmlib):
+    import marshmallow as mm
+    t = mm.render.Textures(seed=0)
+    r = mm.render.Renderer()
+    yield t, r, t.host_all()
+    r.close()
+    t.close()
+
+
+@pytest.mark.parametrize("fmt", ["unorm8", "fp16"])
+def test_precision_sweep_4k(cuda, orc, setup, fmt):
+    import marshmallow as mm
+    import marshmallow.lib as L
+    tex, r, host = setup
+    f = L.FORMAT_FP16 if fmt == "fp16" else L.FORMAT_UNORM8
+    tex.set_density_format(f)
+    rows = []
+    try:
+        for el in (5.0, 30.0, 60.0, 85.0):
+            for off in (-0.2, 0.0, 0.2):
+                p = mm.scene.sweep_params(0)
+                u = mm.scene.uniforms(W, H, yaw=p["yaw"], pitch=p["pitch"], time=p["time"], sun_elevation=el)
+                rgba, dep = render(cuda, r, u, tex, W, H, density_format=f, coverage_offset=off)
+                ref, rdep, _ = orc.march(u, host, W, H, precision=64, coverage_offset=off, rows=(3, H, STEP),
+                                         col_begin=3, col_step=STEP)
+                e = mm.metrics.frame_errors(rgba[3::STEP, 3::STEP], ref, dep[3::STEP, 3::STEP], rdep)
+                rows.append((el, off, e))
+    finally:
+        tex.set_density_format(L.FORMAT_UNORM8)
+    print("\n%s density: elev cov  rmse/255  p99.9/255  max/255  >4/255  depth_med  depth>1e-3" % fmt)
+    for el, off, e in rows:
+        print("  %5.1f %+.1f  %8.4f  %9.4f  %7.2f  %.5f  %.2e  %.4f" % (el, off, e["rmse_255"], e["p999_255"],
+              e["max_255"], e["frac_over_4"], e["depth_rel_median"], e["depth_frac_over_1e3"]))
+    for el, off, e in rows:
+        assert e["nan"] == 0
+        if fmt == "fp16":
+            assert e["rmse_255"] <= 2.0, (el, off, e)
+            assert e["frac_over_4"] <= 0.005, (el, off, e)
+        else:
+            assert e["rmse_255"] <= 1.0, (el, off, e)
+            assert e["p999_255"] <= 4.0, (el, off, e)

@@ -278,6 +278,36 @@ int mm_clouds_march(mm_context ctx, const mm_uniforms* u, const mm_scene_texture
                     const mm_image* out, const mm_march_options* opt, void* stream);
 
 /* ------------------------------------------------------------------------------------------ */
+/* Learned sun-cone surrogate: a 16 -> 64 -> 64 -> 64 -> 1 MLP (ReLU, sigmoid output) trained and  */
+/* run on the tensor cores (tcgen05, BF16 operands, FP32 accumulation).  No counterpart in the     */
+/* reference, whose sun cone (compute-clouds.comp:441-460) is always marched.                      */
+/* ------------------------------------------------------------------------------------------ */
+
+typedef struct mm_mlp_s* mm_mlp;
+
+/* Number of FP32 parameters: W1[64x16], b1[64], W2[64x64], b2[64], W3[64x64], b3[64], w4[64], b4
+ * (row-major [out][in]), in that order. */
+int mm_mlp_param_count(void);
+/* New network on the current device, He-uniform weights from `seed`, zero biases. */
+int mm_mlp_create(uint32_t seed, mm_mlp* out);
+int mm_mlp_destroy(mm_mlp m);
+int mm_mlp_get_params(mm_mlp m, float* host, int n);
+int mm_mlp_set_params(mm_mlp m, const float* host, int n);
+/* y[i] = network(x[i]) for n samples; x: device bf16 [n][16] (16-byte aligned), y: device FP32. */
+int mm_mlp_forward(mm_mlp m, const void* d_x, int n, float* d_y, void* stream);
+/* Gradient of mean((y - t)^2) over the n samples w.r.t. the parameters into d_grad (device, FP32,
+ * mm_mlp_param_count() values); *h_loss (optional) = the loss.  Synchronizes `stream`. */
+int mm_mlp_gradients(mm_mlp m, const void* d_x, const float* d_t, int n, float* d_grad, float* h_loss, void* stream);
+/* `steps` Adam steps (beta 0.9/0.999) of `batch` samples (a multiple of 128) taken in order from
+ * the n samples, wrapping around; h_loss_history (optional, host, `steps` floats) gets each step's
+ * mean squared error.  Synchronizes `stream`. */
+int mm_mlp_train(mm_mlp m, const void* d_x, const float* d_t, int n, int batch, int steps, float lr,
+                 float* h_loss_history, void* stream);
+/* Checkpoint of parameters and Adam state ("MMMLP001" header, count, step, P, M, V). */
+int mm_mlp_save(mm_mlp m, const char* path);
+int mm_mlp_load(mm_mlp m, const char* path);
+
+/* ------------------------------------------------------------------------------------------ */
 /* Diagnostics                                                                                 */
 /* ------------------------------------------------------------------------------------------ */
 
@@ -291,6 +321,14 @@ uint64_t mm_kernel_launch_count(void);
  * (G/s) from `tex2d` (both RGBA textures with texture objects), out[2] FP32 FMA throughput
  * (TFLOP/s).  Synchronizes `stream`.  No reference counterpart (the reference has no timing). */
 int mm_measure_peaks(mm_texture tex3d, mm_texture tex2d, double* out, void* stream);
+
+/* Tensor-core self-check: out[128 x N] = A[128 x K] * B[N x K]^T (bf16 in, FP32 out, row-major,
+ * device pointers) through one tcgen05 MMA pipeline of the surrogate's kernels.  K, N multiples of
+ * 16 in [16, 128].  variant 0 is the operand layout the kernels use; 1 swaps the descriptors'
+ * leading/stride fields.  *d_status is set to 1 if a bounded wait gave up.  No reference
+ * counterpart. */
+int mm_tc_gemm_check(const void* d_a, const void* d_b, int K, int N, int variant, float* d_out, int* d_status,
+                     void* stream);
 
 #ifdef __cplusplus
 }

@@ -100,9 +100,23 @@ SIGNATURES = {
     "mm_context_destroy": (C.c_int, [C.c_void_p]),
     "mm_clouds_march": (C.c_int, [C.c_void_p, C.POINTER(Uniforms), C.POINTER(SceneTextures), C.POINTER(Image),
                                   C.POINTER(MarchOptions), C.c_void_p]),
+    "mm_mlp_param_count": (C.c_int, []),
+    "mm_mlp_create": (C.c_int, [C.c_uint32, C.POINTER(C.c_void_p)]),
+    "mm_mlp_destroy": (C.c_int, [C.c_void_p]),
+    "mm_mlp_get_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "mm_mlp_set_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "mm_mlp_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "mm_mlp_gradients": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_float),
+                                   C.c_void_p]),
+    "mm_mlp_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_void_p,
+                               C.c_void_p]),
+    "mm_mlp_save": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "mm_mlp_load": (C.c_int, [C.c_void_p, C.c_char_p]),
     "mm_last_error_string": (C.c_char_p, []),
     "mm_abi_version": (C.c_int, []),
     "mm_kernel_launch_count": (C.c_uint64, []),
+    "mm_tc_gemm_check": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                   C.c_void_p]),
     "mm_measure_peaks": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double), C.c_void_p]),
 }
 

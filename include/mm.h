@@ -138,6 +138,7 @@ typedef struct mm_noise_desc {
 } mm_noise_desc;
 
 typedef struct mm_texture_s* mm_texture;
+typedef struct mm_mlp_s* mm_mlp; /* the learned sun-cone surrogate (see below) */
 
 /* Generates a noise texture on the GPU into a new library-owned texture (device texels plus
  * a hardware texture object).  Default sizes: low-res 128^3, hi-res 32^3, curl 128^2,
@@ -247,6 +248,13 @@ typedef enum mm_schedule {
                                    lanes, but a warp's texture requests scatter over more texels */
 } mm_schedule;
 
+typedef enum mm_cone_mode {
+    MM_CONE_PLAIN = 0,     /* the six-tap sun cone of compute-clouds.comp:441-453 */
+    MM_CONE_SURROGATE = 1  /* two cone taps + the trained MLP (mm_march_options.surrogate) predict
+                              Beer's transmittance of the six-tap sum; full frames, hardware
+                              sampler, fast math and the tiled schedule only */
+} mm_cone_mode;
+
 typedef struct mm_march_options {
     int pixel_mode;        /* mm_pixel_mode */
     int sampler;           /* mm_sampler_mode */
@@ -258,6 +266,8 @@ typedef struct mm_march_options {
     uint64_t* d_counters;  /* optional device uint64[4]: cloudTest calls, cloudHiRes calls,
                               loop iterations, accumulated samples (atomically added) */
     int schedule;          /* mm_schedule */
+    int cone;              /* mm_cone_mode */
+    mm_mlp surrogate;      /* trained network for MM_CONE_SURROGATE */
 } mm_march_options;
 
 /* Fills `o` with the defaults: full frame, hardware sampler, fast math, UNORM8, offset 0,
@@ -266,8 +276,10 @@ int mm_march_options_default(mm_march_options* o);
 
 typedef struct mm_context_s* mm_context;
 
-/* A context owns the per-device scratch the march uses (work-queue counters).  Create it with
- * the target device current.  Contexts must not be shared by concurrent streams. */
+/* A context owns the per-device scratch the march uses (work-queue counters; for the surrogate
+ * cone, the deferred-sample records: 4 per pixel, ~212 bytes per pixel, allocated by the first
+ * surrogate march of a frame size).  Create it with the target device current.  Contexts must not
+ * be shared by concurrent streams. */
 int mm_context_create(mm_context* out);
 int mm_context_destroy(mm_context ctx);
 
@@ -282,8 +294,6 @@ int mm_clouds_march(mm_context ctx, const mm_uniforms* u, const mm_scene_texture
 /* run on the tensor cores (tcgen05, BF16 operands, FP32 accumulation).  No counterpart in the     */
 /* reference, whose sun cone (compute-clouds.comp:441-460) is always marched.                      */
 /* ------------------------------------------------------------------------------------------ */
-
-typedef struct mm_mlp_s* mm_mlp;
 
 /* Number of FP32 parameters: W1[64x16], b1[64], W2[64x64], b2[64], W3[64x64], b3[64], w4[64], b4
  * (row-major [out][in]), in that order. */
@@ -303,6 +313,15 @@ int mm_mlp_gradients(mm_mlp m, const void* d_x, const float* d_t, int n, float* 
  * mean squared error.  Synchronizes `stream`. */
 int mm_mlp_train(mm_mlp m, const void* d_x, const float* d_t, int n, int batch, int steps, float lr,
                  float* h_loss_history, void* stream);
+/* Training samples for the surrogate: for each texture seed first_seed .. first_seed+n_seeds-1
+ * (the four seeded textures regenerated on the GPU), `per_seed` samples at uniform random points
+ * of the cloud layer within +-half_extent m of the origin where the march would accumulate, with a
+ * random sun (elevation 0-90 deg, any azimuth) and wind time in [0, 2] s; features as the surrogate
+ * march computes them (d_x: bf16 [n_seeds*per_seed][16]) and the target exp(-sum of the plain
+ * six-tap cone) (d_t: FP32).  *produced = samples written.  Synchronizes `stream`. */
+int mm_surrogate_generate(uint32_t first_seed, int n_seeds, int per_seed, float half_extent, void* d_x,
+                          float* d_t, int* produced, void* stream);
+
 /* Checkpoint of parameters and Adam state ("MMMLP001" header, count, step, P, M, V). */
 int mm_mlp_save(mm_mlp m, const char* path);
 int mm_mlp_load(mm_mlp m, const char* path);

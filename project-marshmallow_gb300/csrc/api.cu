@@ -159,6 +159,24 @@ int make_texture(int w, int h, int d, int ch, mm_texture* out) {
     return MM_OK;
 }
 
+}  // namespace
+
+mm::TexView mm::texture_view(mm_texture t) {
+    mm::TexView v;
+    memset(&v, 0, sizeof(v));
+    if (t) {
+        v.tex = t->tex;
+        v.texels = t->texels;
+        v.w = t->width;
+        v.h = t->height;
+        v.d = t->depth;
+        v.channels = t->channels;
+    }
+    return v;
+}
+
+namespace {
+
 mm::TexView view_of(mm_texture t) {
     mm::TexView v;
     memset(&v, 0, sizeof(v));
@@ -317,8 +335,61 @@ int mm_context_create(mm_context* out) {
 int mm_context_destroy(mm_context c) {
     if (!c) return fail(MM_ERR_INVALID_ARGUMENT, "context: null handle");
     if (c->d_work) cudaFree(c->d_work);
+    cudaFree(c->sur_x);
+    cudaFree(c->sur_meta);
+    cudaFree(c->sur_y);
+    cudaFree(c->sur_ray);
     delete c;
     return MM_OK;
+}
+
+int mm_surrogate_generate(uint32_t first_seed, int n_seeds, int per_seed, float half_extent, void* d_x, float* d_t,
+                          int* produced, void* stream) {
+    if (!d_x || !d_t || n_seeds <= 0 || per_seed <= 0 || !(half_extent > 0.0f) ||
+        (long long)n_seeds * per_seed > 0x7fffffffLL)
+        return fail(MM_ERR_INVALID_ARGUMENT, "surrogate samples: bad arguments");
+    if (((uintptr_t)d_x) % 16) return fail(MM_ERR_INVALID_ARGUMENT, "surrogate samples: features must be 16-byte aligned");
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned int* d_count = nullptr;
+    MM_CUDA_TRY(cudaMalloc(&d_count, sizeof(unsigned int)));
+    int total = 0, r = MM_OK;
+    for (int k = 0; k < n_seeds && r == MM_OK; ++k) {
+        const uint32_t seed = first_seed + (uint32_t)k;
+        mm_texture t[4] = {nullptr, nullptr, nullptr, nullptr};
+        const int kinds[4] = {MM_NOISE_WEATHER, MM_NOISE_CURL2D, MM_NOISE_LOWRES_PERLIN_WORLEY, MM_NOISE_HIRES_WORLEY};
+        for (int i = 0; i < 4 && r == MM_OK; ++i) {
+            mm_noise_desc d = {kinds[i], seed, 0, 0, 0};
+            r = mm_noise_generate(&d, &t[i], stream);
+        }
+        if (r == MM_OK) {
+            mm::MarchLaunch p;
+            memset(&p, 0, sizeof(p));
+            p.weather = mm::texture_view(t[0]);
+            p.curl = mm::texture_view(t[1]);
+            p.low = mm::texture_view(t[2]);
+            p.hi = mm::texture_view(t[3]);
+            uint8_t* xk = (uint8_t*)d_x + (size_t)total * 16 * 2;
+            float* tk = d_t + total;
+            cudaError_t e = cudaMemsetAsync(d_count, 0, sizeof(unsigned int), s);
+            if (e != cudaSuccess) r = mm::cuda_fail(e, "surrogate count reset");
+            unsigned int got = 0;
+            const unsigned long long chunk = 1ull << 23;
+            for (unsigned long long first = 0; r == MM_OK && got < (unsigned)per_seed && first < (1ull << 32);
+                 first += chunk) {
+                r = mm::launch_surrogate_samples(p, seed, first, chunk, half_extent, xk, tk, d_count, per_seed, s);
+                if (r == MM_OK && (e = cudaMemcpyAsync(&got, d_count, sizeof(got), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+                    r = mm::cuda_fail(e, "surrogate count");
+                if (r == MM_OK && (e = cudaStreamSynchronize(s)) != cudaSuccess) r = mm::cuda_fail(e, "surrogate samples");
+            }
+            total += got < (unsigned)per_seed ? (int)got : per_seed;
+        }
+        cudaStreamSynchronize(s);
+        for (int i = 0; i < 4; ++i)
+            if (t[i]) mm_texture_destroy(t[i]);
+    }
+    cudaFree(d_count);
+    if (produced) *produced = total;
+    return r;
 }
 
 int mm_march_options_default(mm_march_options* o) {
@@ -346,6 +417,14 @@ int mm_clouds_march(mm_context ctx, const mm_uniforms* u, const mm_scene_texture
     if (o.math != MM_MATH_FAST && o.math != MM_MATH_EXACT) return fail(MM_ERR_INVALID_ARGUMENT, "march: bad math %d", o.math);
     if (o.schedule != MM_SCHEDULE_PERSISTENT && o.schedule != MM_SCHEDULE_TILED)
         return fail(MM_ERR_INVALID_ARGUMENT, "march: bad schedule %d", o.schedule);
+    if (o.cone != MM_CONE_PLAIN && o.cone != MM_CONE_SURROGATE) return fail(MM_ERR_INVALID_ARGUMENT, "march: bad cone %d", o.cone);
+    if (o.cone == MM_CONE_SURROGATE) {
+        if (!o.surrogate) return fail(MM_ERR_INVALID_ARGUMENT, "march: surrogate cone without a network");
+        if (o.pixel_mode != MM_PIXELS_FULL || o.sampler != MM_SAMPLER_HARDWARE || o.math != MM_MATH_FAST ||
+            o.schedule != MM_SCHEDULE_TILED)
+            return fail(MM_ERR_UNSUPPORTED, "march: the surrogate cone runs full frames with the hardware sampler, "
+                                            "fast math and the tiled schedule");
+    }
     if (o.density_format < MM_FORMAT_UNORM8 || o.density_format > MM_FORMAT_BF16)
         return fail(MM_ERR_INVALID_ARGUMENT, "march: bad density_format %d", o.density_format);
     if (!(o.coverage_offset == o.coverage_offset) || o.coverage_offset < -1.0f || o.coverage_offset > 1.0f)
@@ -403,6 +482,7 @@ int mm_clouds_march(mm_context ctx, const mm_uniforms* u, const mm_scene_texture
     p.coverage_offset = o.coverage_offset;
     p.counters = reinterpret_cast<unsigned long long*>(o.d_counters);
     cudaStream_t s = (cudaStream_t)stream;
+    if (o.cone == MM_CONE_SURROGATE) return mm::launch_surrogate_frame(p, ctx, o.surrogate, s);
     if (o.math == MM_MATH_EXACT) return mm::launch_march_exact(p, o.sampler, o.schedule, ctx->d_work, ctx->num_sms, s);
     return mm::launch_march_fast(p, o.sampler, o.density_format, o.schedule, ctx->d_work, ctx->num_sms, s);
 }

@@ -172,11 +172,13 @@ struct InferSmem {
     uint32_t tslot;
 };
 
-__global__ void __launch_bounds__(128, 1) infer_kernel(const __nv_bfloat16* __restrict__ X, int n,
+__global__ void __launch_bounds__(128, 4) infer_kernel(const __nv_bfloat16* __restrict__ X, int n,
+                                                       const unsigned int* __restrict__ n_dev,
                                                        const float* __restrict__ P, const __nv_bfloat16* __restrict__ WB,
                                                        float* __restrict__ Y, int* status) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
+    if (n_dev) n = min(n, (int)*n_dev);  // sample count written by an earlier kernel
     const int tid = threadIdx.x, warp = tid >> 5;
     load_weights(S.w, P, WB);
     if (tid == 0) tc::mbar_init(&S.bar, 1);
@@ -529,6 +531,26 @@ int run_train(mm_mlp m, const void* X, const float* T, int n, int tile0, int til
 
 }  // namespace
 
+namespace mm {
+
+// Inference on up to `cap` samples, the actual count read from device memory (surrogate march).
+int mlp_infer_device_count(mm_mlp m, const void* d_x, int cap, const unsigned int* d_count, float* d_y,
+                           cudaStream_t s) {
+    int r = set_smem_limits();
+    if (r) return r;
+    const int tiles = (cap + 127) / 128;
+    const int grid = tiles < 4 * m->num_sms ? tiles : 4 * m->num_sms;
+    mlp::infer_kernel<<<grid, 128, infer_smem(), s>>>((const __nv_bfloat16*)d_x, cap, d_count, m->P, m->WB, d_y,
+                                                      m->status);
+    MM_CUDA_TRY(cudaGetLastError());
+    count_launch();
+    return MM_OK;
+}
+
+int* mlp_status_ptr(mm_mlp m) { return m->status; }
+
+}  // namespace mm
+
 extern "C" {
 
 int mm_mlp_param_count(void) { return mm::mlp::kParams; }
@@ -618,8 +640,9 @@ int mm_mlp_forward(mm_mlp m, const void* d_x, int n, float* d_y, void* stream) {
     if (r) return r;
     cudaStream_t s = (cudaStream_t)stream;
     const int tiles = (n + 127) / 128;
-    const int grid = tiles < m->num_sms ? tiles : m->num_sms;
-    mm::mlp::infer_kernel<<<grid, 128, infer_smem(), s>>>((const __nv_bfloat16*)d_x, n, m->P, m->WB, d_y, m->status);
+    const int grid = tiles < 4 * m->num_sms ? tiles : 4 * m->num_sms;
+    mm::mlp::infer_kernel<<<grid, 128, infer_smem(), s>>>((const __nv_bfloat16*)d_x, n, nullptr, m->P, m->WB, d_y,
+                                                          m->status);
     MM_CUDA_TRY(cudaGetLastError());
     mm::count_launch();
     return MM_OK;

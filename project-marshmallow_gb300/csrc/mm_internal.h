@@ -44,8 +44,14 @@ struct mm_texture_s {
 
 struct mm_context_s {
     int device = 0;
-    unsigned int* d_work = nullptr;  // work-queue counters of the persistent march
+    unsigned int* d_work = nullptr;  // [0] persistent-march tile counter, [1] surrogate record count
     int num_sms = 0;
+    // surrogate-cone records (surrogate.cu)
+    void* sur_x = nullptr;
+    void* sur_meta = nullptr;
+    void* sur_y = nullptr;
+    void* sur_ray = nullptr;
+    size_t sur_cap = 0, sur_pixels = 0;
 };
 
 namespace mm {
@@ -82,6 +88,18 @@ int launch_march_fast(const MarchLaunch& p, int sampler, int format, int schedul
 int launch_noise(int kind, uint32_t seed, int w, int h, int d, uint8_t* out, cudaStream_t s);
 int launch_ref_curl(uint8_t* out_rgba, float* scratch_curl, float* scratch_bounds, cudaStream_t s);
 int launch_hash_stage(int which, const void* in, uint32_t seed, size_t n, void* out, cudaStream_t s);
+
+// Surrogate network (mlp.cu): inference over a sample count held in device memory.
+int mlp_infer_device_count(mm_mlp m, const void* d_x, int cap, const unsigned int* d_count, float* d_y,
+                           cudaStream_t s);
+int* mlp_status_ptr(mm_mlp m);
+
+// Surrogate march and training samples (surrogate.cu).
+int launch_surrogate_frame(const MarchLaunch& p, mm_context ctx, mm_mlp net, cudaStream_t s);
+int launch_surrogate_samples(const MarchLaunch& p, uint32_t seed, unsigned long long first, unsigned long long n,
+                             float half_extent, void* d_x, float* d_t, unsigned int* d_count, int cap,
+                             cudaStream_t s);
+TexView texture_view(mm_texture t);
 
 #endif  // CUDA runtime available
 

@@ -23,6 +23,7 @@ PIXELS_FULL, PIXELS_PHASE16 = range(2)
 SAMPLER_HARDWARE, SAMPLER_SOFTWARE = range(2)
 MATH_FAST, MATH_EXACT = range(2)
 SCHEDULE_TILED, SCHEDULE_PERSISTENT = range(2)
+CONE_PLAIN, CONE_SURROGATE = range(2)
 
 F16 = C.c_float * 16
 F4 = C.c_float * 4
@@ -74,7 +75,7 @@ class Image(C.Structure):
 class MarchOptions(C.Structure):
     _fields_ = [("pixel_mode", C.c_int), ("sampler", C.c_int), ("math", C.c_int),
                 ("density_format", C.c_int), ("coverage_offset", C.c_float), ("ref_uv_1080p", C.c_int),
-                ("d_counters", C.c_void_p), ("schedule", C.c_int)]
+                ("d_counters", C.c_void_p), ("schedule", C.c_int), ("cone", C.c_int), ("surrogate", C.c_void_p)]
 
 
 # Every function include/mm.h declares, with its ctypes signature.
@@ -110,6 +111,8 @@ SIGNATURES = {
                                    C.c_void_p]),
     "mm_mlp_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_void_p,
                                C.c_void_p]),
+    "mm_surrogate_generate": (C.c_int, [C.c_uint32, C.c_int, C.c_int, C.c_float, C.c_void_p, C.c_void_p,
+                                        C.POINTER(C.c_int), C.c_void_p]),
     "mm_mlp_save": (C.c_int, [C.c_void_p, C.c_char_p]),
     "mm_mlp_load": (C.c_int, [C.c_void_p, C.c_char_p]),
     "mm_last_error_string": (C.c_char_p, []),

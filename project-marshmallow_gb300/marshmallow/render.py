@@ -101,13 +101,15 @@ class Renderer:
 
     @staticmethod
     def options(pixel_mode=L.PIXELS_FULL, sampler=L.SAMPLER_HARDWARE, math=L.MATH_FAST, density_format=L.FORMAT_UNORM8,
-                coverage_offset=0.0, ref_uv_1080p=0, counters=None, schedule=L.SCHEDULE_TILED):
+                coverage_offset=0.0, ref_uv_1080p=0, counters=None, schedule=L.SCHEDULE_TILED, surrogate=None):
         o = L.MarchOptions()
         L.load().mm_march_options_default(C.byref(o))
         o.pixel_mode, o.sampler, o.math, o.density_format = pixel_mode, sampler, math, density_format
         o.coverage_offset, o.ref_uv_1080p = coverage_offset, ref_uv_1080p
         o.d_counters = counters.data_ptr() if counters is not None else None
         o.schedule = schedule
+        o.cone = L.CONE_SURROGATE if surrogate is not None else L.CONE_PLAIN
+        o.surrogate = surrogate
         return o
 
     def march(self, u, textures, rgba, depth=None, stream=None, **opts):

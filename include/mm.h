@@ -290,6 +290,39 @@ int mm_clouds_march(mm_context ctx, const mm_uniforms* u, const mm_scene_texture
                     const mm_image* out, const mm_march_options* opt, void* stream);
 
 /* ------------------------------------------------------------------------------------------ */
+/* Many views in one launch.  No counterpart in the reference, which renders one camera.          */
+/* ------------------------------------------------------------------------------------------ */
+
+/* One view of a batch: its own uniform blocks (camera, sun, wind/time) and output image. */
+typedef struct mm_view {
+    mm_uniforms u;
+    mm_image out;
+    float coverage_offset;
+} mm_view;
+
+typedef struct mm_batch_options {
+    int warp_tile_w;    /* pixels across one warp's 32-ray tile: 4, 8 (default), 16 or 32 */
+    int tiles_per_grab; /* warp tiles a warp takes from the shared queue at a time, 1..64 (default 4) */
+    int use_graph;      /* 1 (default): replay a captured CUDA graph (upload, reset, kernel) */
+} mm_batch_options;
+
+int mm_batch_options_default(mm_batch_options* o);
+
+/* Renders n views (full frames, hardware sampler, fast math, plain cone) with the shared textures in
+ * one persistent kernel: warps take tiles of all views from one queue.  The host-side records are
+ * staged in pinned memory owned by the context; a call waits for the previous batch of the same
+ * context to finish reading them.  The graph is re-captured when the view count or the options
+ * change. */
+int mm_clouds_march_batch(mm_context ctx, const mm_view* views, int n, const mm_scene_textures* tex,
+                          const mm_batch_options* opt, void* stream);
+
+/* Autotuner: times warp_tile_w in {4, 8, 16, 32} x tiles_per_grab in {1, 2, 4, 8, 16} on this batch
+ * (ms_table, optional: 20 floats, row-major in that order) and returns the fastest options.
+ * Synchronizes `stream`. */
+int mm_batch_autotune(mm_context ctx, const mm_view* views, int n, const mm_scene_textures* tex,
+                      mm_batch_options* best, float* ms_table, void* stream);
+
+/* ------------------------------------------------------------------------------------------ */
 /* Learned sun-cone surrogate: a 16 -> 64 -> 64 -> 64 -> 1 MLP (ReLU, sigmoid output) trained and  */
 /* run on the tensor cores (tcgen05, BF16 operands, FP32 accumulation).  No counterpart in the     */
 /* reference, whose sun cone (compute-clouds.comp:441-460) is always marched.                      */

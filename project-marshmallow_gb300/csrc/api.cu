@@ -334,6 +334,7 @@ int mm_context_create(mm_context* out) {
 
 int mm_context_destroy(mm_context c) {
     if (!c) return fail(MM_ERR_INVALID_ARGUMENT, "context: null handle");
+    mm::batch_state_destroy(c);
     if (c->d_work) cudaFree(c->d_work);
     cudaFree(c->sur_x);
     cudaFree(c->sur_meta);
@@ -402,14 +403,13 @@ int mm_march_options_default(mm_march_options* o) {
     return MM_OK;
 }
 
-int mm_clouds_march(mm_context ctx, const mm_uniforms* u, const mm_scene_textures* tex, const mm_image* out,
-                    const mm_march_options* opt, void* stream) {
-    if (!ctx || !u || !tex || !out) return fail(MM_ERR_INVALID_ARGUMENT, "march: null argument");
-    mm_march_options o;
-    if (opt)
-        o = *opt;
-    else
-        mm_march_options_default(&o);
+}  // extern "C"
+
+// Checks one march request (the argument contract of mm_clouds_march).
+int mm::validate_march(mm_context ctx, const mm_uniforms* u, const mm_scene_textures* tex, const mm_image* out,
+                       const mm_march_options* opt) {
+    if (!ctx || !u || !tex || !out || !opt) return fail(MM_ERR_INVALID_ARGUMENT, "march: null argument");
+    const mm_march_options& o = *opt;
     if (o.pixel_mode != MM_PIXELS_FULL && o.pixel_mode != MM_PIXELS_PHASE16)
         return fail(MM_ERR_INVALID_ARGUMENT, "march: bad pixel_mode %d", o.pixel_mode);
     if (o.sampler != MM_SAMPLER_HARDWARE && o.sampler != MM_SAMPLER_SOFTWARE)
@@ -460,27 +460,47 @@ int mm_clouds_march(mm_context ctx, const mm_uniforms* u, const mm_scene_texture
     if (o.density_format == MM_FORMAT_UNORM8 && o.sampler == MM_SAMPLER_HARDWARE &&
         (tex->low_res->format != MM_FORMAT_UNORM8 || tex->hi_res->format != MM_FORMAT_UNORM8))
         return fail(MM_ERR_INVALID_ARGUMENT, "march: density textures are not UNORM8");
+    return MM_OK;
+}
 
-    mm::MarchLaunch p;
+// The kernel-side record of one view.
+void mm::fill_march_launch(const mm_uniforms& u, const mm_scene_textures* tex, const mm_image& out,
+                           const mm_march_options& o, MarchLaunch* pp) {
+    MarchLaunch& p = *pp;
     memset(&p, 0, sizeof(p));
-    p.u = *u;
+    p.u = u;
     p.weather = view_of(tex->weather);
     p.night = view_of(tex->night_sky);
     p.curl = view_of(tex->curl);
     p.low = view_of(tex->low_res);
     p.hi = view_of(tex->hi_res);
-    p.rgba = reinterpret_cast<float4*>(out->rgba);
-    p.rgba_pitch = out->rgba_pitch_bytes;
-    p.depth = out->depth;
-    p.depth_pitch = out->depth_pitch_bytes;
-    p.width = out->width;
-    p.height = out->height;
+    p.rgba = reinterpret_cast<float4*>(out.rgba);
+    p.rgba_pitch = out.rgba_pitch_bytes;
+    p.depth = out.depth;
+    p.depth_pitch = out.depth_pitch_bytes;
+    p.width = out.width;
+    p.height = out.height;
     p.pixel_mode = o.pixel_mode;
-    p.phase = (int)ph;
-    p.uv_w = o.ref_uv_1080p ? 1920.0f : (float)out->width;
-    p.uv_h = o.ref_uv_1080p ? 1080.0f : (float)out->height;
+    p.phase = (int)u.sun.color[3];
+    p.uv_w = o.ref_uv_1080p ? 1920.0f : (float)out.width;
+    p.uv_h = o.ref_uv_1080p ? 1080.0f : (float)out.height;
     p.coverage_offset = o.coverage_offset;
     p.counters = reinterpret_cast<unsigned long long*>(o.d_counters);
+}
+
+extern "C" {
+
+int mm_clouds_march(mm_context ctx, const mm_uniforms* u, const mm_scene_textures* tex, const mm_image* out,
+                    const mm_march_options* opt, void* stream) {
+    mm_march_options o;
+    if (opt)
+        o = *opt;
+    else
+        mm_march_options_default(&o);
+    int r = mm::validate_march(ctx, u, tex, out, &o);
+    if (r) return r;
+    mm::MarchLaunch p;
+    mm::fill_march_launch(*u, tex, *out, o, &p);
     cudaStream_t s = (cudaStream_t)stream;
     if (o.cone == MM_CONE_SURROGATE) return mm::launch_surrogate_frame(p, ctx, o.surrogate, s);
     if (o.math == MM_MATH_EXACT) return mm::launch_march_exact(p, o.sampler, o.schedule, ctx->d_work, ctx->num_sms, s);

@@ -639,7 +639,8 @@ __device__ __forceinline__ void flush_work(unsigned long long* cnt, const Work& 
 
 // The whole of main() (:288-500) for pixel (px, py) in one thread, the shader's own loop structure.
 template <bool E, int S>
-__device__ void march_pixel(const MarchLaunch& p, const Frame& f, const V3* cone, int px, int py, Work& w) {
+__device__ __forceinline__ void march_pixel(const MarchLaunch& p, const Frame& f, const V3* cone, int px, int py,
+                                            Work& w) {
     const Ray r = ray_setup<E, S>(p, f, px, py);
     if (r.killed) {
         store_pixel(p, px, py, make_float4(r.bg.x, r.bg.y, r.bg.z, r.alpha), CUDART_INF_F);

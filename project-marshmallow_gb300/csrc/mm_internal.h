@@ -52,6 +52,7 @@ struct mm_context_s {
     void* sur_y = nullptr;
     void* sur_ray = nullptr;
     size_t sur_cap = 0, sur_pixels = 0;
+    void* batch = nullptr;  // multi-view launch state (batch.cu)
 };
 
 namespace mm {
@@ -100,6 +101,13 @@ int launch_surrogate_samples(const MarchLaunch& p, uint32_t seed, unsigned long 
                              float half_extent, void* d_x, float* d_t, unsigned int* d_count, int cap,
                              cudaStream_t s);
 TexView texture_view(mm_texture t);
+
+// Argument contract of mm_clouds_march and the kernel record of one view (api.cu).
+int validate_march(mm_context ctx, const mm_uniforms* u, const mm_scene_textures* tex, const mm_image* out,
+                   const mm_march_options* opt);
+void fill_march_launch(const mm_uniforms& u, const mm_scene_textures* tex, const mm_image& out,
+                       const mm_march_options& o, MarchLaunch* p);
+void batch_state_destroy(mm_context ctx);
 
 #endif  // CUDA runtime available
 

@@ -78,6 +78,14 @@ class MarchOptions(C.Structure):
                 ("d_counters", C.c_void_p), ("schedule", C.c_int), ("cone", C.c_int), ("surrogate", C.c_void_p)]
 
 
+class View(C.Structure):
+    _fields_ = [("u", Uniforms), ("out", Image), ("coverage_offset", C.c_float)]
+
+
+class BatchOptions(C.Structure):
+    _fields_ = [("warp_tile_w", C.c_int), ("tiles_per_grab", C.c_int), ("use_graph", C.c_int)]
+
+
 # Every function include/mm.h declares, with its ctypes signature.
 SIGNATURES = {
     "mm_camera_from_angles": (C.c_int, [C.POINTER(C.c_float), C.c_float, C.c_float, C.c_float, C.c_int, C.c_int,
@@ -101,6 +109,11 @@ SIGNATURES = {
     "mm_context_destroy": (C.c_int, [C.c_void_p]),
     "mm_clouds_march": (C.c_int, [C.c_void_p, C.POINTER(Uniforms), C.POINTER(SceneTextures), C.POINTER(Image),
                                   C.POINTER(MarchOptions), C.c_void_p]),
+    "mm_batch_options_default": (C.c_int, [C.POINTER(BatchOptions)]),
+    "mm_clouds_march_batch": (C.c_int, [C.c_void_p, C.POINTER(View), C.c_int, C.POINTER(SceneTextures),
+                                        C.POINTER(BatchOptions), C.c_void_p]),
+    "mm_batch_autotune": (C.c_int, [C.c_void_p, C.POINTER(View), C.c_int, C.POINTER(SceneTextures),
+                                    C.POINTER(BatchOptions), C.c_void_p, C.c_void_p]),
     "mm_mlp_param_count": (C.c_int, []),
     "mm_mlp_create": (C.c_int, [C.c_uint32, C.POINTER(C.c_void_p)]),
     "mm_mlp_destroy": (C.c_int, [C.c_void_p]),

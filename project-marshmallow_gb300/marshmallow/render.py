@@ -122,6 +122,28 @@ class Renderer:
         L.check(self.lib.mm_clouds_march(self.ctx, C.byref(u), C.byref(st), C.byref(img), C.byref(o),
                                          _stream_ptr(stream)), "mm_clouds_march")
 
+    def march_batch(self, views, textures, outputs, stream=None, warp_tile_w=8, tiles_per_grab=4, use_graph=1):
+        """views: (width, height, uniforms) triples; outputs: matching (rgba, depth) CUDA tensors."""
+        arr = (L.View * len(views))()
+        for i, ((w, h, u), (rgba, dep)) in enumerate(zip(views, outputs)):
+            arr[i].u = u
+            arr[i].out = L.Image(rgba.data_ptr(), rgba.stride(0) * 4, dep.data_ptr() if dep is not None else None,
+                                 dep.stride(0) * 4 if dep is not None else 0, w, h)
+            arr[i].coverage_offset = 0.0
+        o = L.BatchOptions(warp_tile_w, tiles_per_grab, use_graph)
+        st = textures.scene() if isinstance(textures, Textures) else textures
+        L.check(self.lib.mm_clouds_march_batch(self.ctx, arr, len(views), C.byref(st), C.byref(o), _stream_ptr(stream)),
+                "mm_clouds_march_batch")
+        return arr
+
+    def autotune_batch(self, views_arr, n, textures, stream=None):
+        st = textures.scene() if isinstance(textures, Textures) else textures
+        best = L.BatchOptions()
+        table = (C.c_float * 20)()
+        L.check(self.lib.mm_batch_autotune(self.ctx, views_arr, n, C.byref(st), C.byref(best), table,
+                                           _stream_ptr(stream)), "mm_batch_autotune")
+        return best, list(table)
+
     def close(self):
         if self.ctx:
             self.lib.mm_context_destroy(self.ctx)

@@ -29,3 +29,28 @@ def sweep_uniforms(k, width, height, n=16, sun_elevation=30.0, sun_azimuth=0.0):
     p = sweep_params(k, n)
     return uniforms(width, height, yaw=p["yaw"], pitch=p["pitch"], time=p["time"], sun_elevation=sun_elevation,
                     sun_azimuth=sun_azimuth)
+
+
+def cubemap_views(size=512, eye=(0.0, 10.0, 0.0), time=0.0, sun_elevation=30.0, sun_azimuth=0.0):
+    """Six cube-map probe faces (+x, -x, +y, -y, +z, -z) at `size`^2 with a 90 degree field of view."""
+    faces = [(0.0, 0.0), (180.0, 0.0), (0.0, 89.9), (0.0, -89.9), (90.0, 0.0), (270.0, 0.0)]
+    return [(size, size, uniforms(size, size, eye=eye, yaw=y, pitch=p, fov=90.0, time=time, sun_elevation=sun_elevation,
+                                  sun_azimuth=sun_azimuth)) for y, p in faces]
+
+
+def batch_views(seed=0):
+    """The uneven-view batch: 6 cube-map faces at 512^2, 32 cameras at random resolutions between
+    640x360 and 1920x1080 and 32 cameras at 3840x2160 with random sun elevation 5-85 deg and yaw
+    0-360 deg (seeded).  Returns (width, height, uniforms) triples."""
+    import random
+    rng = random.Random(seed)
+    views = cubemap_views()
+    for _ in range(32):
+        w = rng.randrange(640, 1921) // 16 * 16
+        h = max(360, min(1080, int(w * 9 / 16)))
+        views.append((w, h, uniforms(w, h, yaw=rng.uniform(0.0, 360.0), pitch=rng.uniform(5.0, 25.0),
+                                     time=rng.uniform(0.0, 2.0))))
+    for _ in range(32):
+        views.append((3840, 2160, uniforms(3840, 2160, yaw=rng.uniform(0.0, 360.0), pitch=rng.uniform(5.0, 25.0),
+                                           time=rng.uniform(0.0, 2.0), sun_elevation=rng.uniform(5.0, 85.0))))
+    return views

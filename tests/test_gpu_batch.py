@@ -1,0 +1,85 @@
+"""Many views in one persistent, graph-captured launch (mm_clouds_march_batch) and its autotuner."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def env(cuda, mmlib):
+    import marshmallow as mm
+    t = mm.render.Textures(seed=0)
+    r = mm.render.Renderer()
+    yield t, r
+    r.close()
+    t.close()
+
+
+def _outputs(cuda, views):
+    return [(cuda.zeros((h, w, 4), device="cuda"), cuda.zeros((h, w), device="cuda")) for w, h, _ in views]
+
+
+def test_batch_equals_single_views(cuda, env):
+    import marshmallow as mm
+    tex, r = env
+    views = mm.scene.cubemap_views(128) + [(320, 180, mm.scene.uniforms(320, 180, yaw=40.0, pitch=20.0)),
+                                          (257, 131, mm.scene.uniforms(257, 131, yaw=200.0, pitch=8.0, time=1.0,
+                                                                       sun_elevation=70.0))]
+    for tw, grab in ((8, 4), (4, 1), (32, 16)):
+        outs = _outputs(cuda, views)
+        r.march_batch(views, tex, outs, warp_tile_w=tw, tiles_per_grab=grab)
+        cuda.cuda.synchronize()
+        for (w, h, u), (rgba, dep) in zip(views, outs):
+            ref = cuda.zeros((h, w, 4), device="cuda")
+            rdep = cuda.zeros((h, w), device="cuda")
+            r.march(u, tex, ref, rdep)
+            cuda.cuda.synchronize()
+            e = mm.metrics.frame_errors(rgba.cpu().numpy(), ref.cpu().numpy(), dep.cpu().numpy(), rdep.cpu().numpy())
+            assert e["rmse_255"] < 0.05 and e["frac_over_4"] < 1e-3, (tw, grab, w, h, e)
+
+
+def test_graph_replay_takes_new_uniforms(cuda, env):
+    import marshmallow as mm
+    tex, r = env
+    a = [(200, 100, mm.scene.uniforms(200, 100, yaw=0.0, pitch=15.0))]
+    b = [(200, 100, mm.scene.uniforms(200, 100, yaw=120.0, pitch=10.0, sun_elevation=60.0))]
+    outs = _outputs(cuda, a)
+    r.march_batch(a, tex, outs)
+    first = outs[0][0].cpu().numpy()
+    r.march_batch(b, tex, outs)  # same shape and options: the captured graph is replayed
+    second = outs[0][0].cpu().numpy()
+    ref = cuda.zeros((100, 200, 4), device="cuda")
+    r.march(b[0][2], tex, ref)
+    cuda.cuda.synchronize()
+    assert not np.array_equal(first, second)
+    assert mm.metrics.frame_errors(second, ref.cpu().numpy())["rmse_255"] < 0.05
+
+
+def test_uneven_batch_and_autotune(cuda, env):
+    """The 70-view batch (cube map, 32 mid-size cameras, 32 4K cameras): one launch vs one launch per
+    view, and the autotuner's pick."""
+    import marshmallow as mm
+    tex, r = env
+    views = mm.scene.batch_views(seed=0)
+    assert len(views) == 70
+    outs = _outputs(cuda, views)
+    arr = r.march_batch(views, tex, outs)
+    best, table = r.autotune_batch(arr, len(views), tex)
+    cuda.cuda.synchronize()
+    ev = [cuda.cuda.Event(enable_timing=True) for _ in range(4)]
+    ev[0].record()
+    r.march_batch(views, tex, outs, warp_tile_w=best.warp_tile_w, tiles_per_grab=best.tiles_per_grab)
+    ev[1].record()
+    for (w, h, u), (rgba, dep) in zip(views, outs):
+        r.march(u, tex, rgba, dep)
+    ev[2].record()
+    cuda.cuda.synchronize()
+    t_batch, t_seq = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+    rays = sum(w * h for w, h, _ in views)
+    print("\n70 views, %.1f Mrays: batch %.2f ms (%.0f Mrays/s, warp tile %d, grab %d) vs per-view %.2f ms"
+          % (rays / 1e6, t_batch, rays / t_batch / 1e3, best.warp_tile_w, best.tiles_per_grab, t_seq))
+    print("autotune table (ms; rows warp_tile_w 4/8/16/32, cols grab 1/2/4/8/16):")
+    for i in range(4):
+        print("  " + " ".join("%8.2f" % v for v in table[5 * i:5 * i + 5]))
+    assert best.warp_tile_w in (4, 8, 16, 32) and 1 <= best.tiles_per_grab <= 16
+    assert all(v > 0 for v in table)

@@ -58,6 +58,8 @@ def load():
         lib.oracle_hash3.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_uint32]
         lib.oracle_hash3.restype = C.c_uint32
         lib.oracle_tonemap.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p]
+        lib.oracle_reproject_f32.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                             C.c_void_p]
         _lib = lib
     return _lib
 
@@ -121,3 +123,17 @@ def tonemap(rgba):
     out = np.zeros(a.shape[:-1] + (3,), np.float32)
     load().oracle_tonemap(a.ctypes.data, a.size // 4, out.ctypes.data)
     return out
+
+
+def reproject(uniforms, src_rgba, src_depth=None):
+    """reproject.comp over a frame: returns (rgba, depth) from the previous frame's images."""
+    h, w = src_rgba.shape[:2]
+    src = np.ascontiguousarray(src_rgba, np.float32)
+    sd = np.ascontiguousarray(src_depth, np.float32) if src_depth is not None else None
+    out = np.zeros_like(src)
+    od = np.zeros((h, w), np.float32) if sd is not None else None
+    rc = load().oracle_reproject_f32(C.addressof(uniforms), src.ctypes.data, sd.ctypes.data if sd is not None else None,
+                                     w, h, out.ctypes.data, od.ctypes.data if od is not None else None)
+    if rc:
+        raise RuntimeError("oracle reproject failed: %d" % rc)
+    return out, od

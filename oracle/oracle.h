@@ -70,6 +70,11 @@ int oracle_noise_fill(int kind, uint32_t seed, int w, int h, int d, uint8_t* out
 uint32_t oracle_hash32(uint32_t x);
 uint32_t oracle_hash3(int32_t x, int32_t y, int32_t z, uint32_t s);
 
+/* reproject.comp:91-152 over a w x h frame: dst from src (rgba float4 rows; depth optional) with the
+ * camera and camera_prev blocks of u.  Depth (new) follows the centre tap, as alpha does. */
+int oracle_reproject_f32(const mm_uniforms* u, const float* src_rgba, const float* src_depth, int w, int h,
+                         float* dst_rgba, float* dst_depth);
+
 /* Uncharted-2 tonemap of tonemap.frag:10-28 (exposure 0.7, white 50.2, gamma 1/2.2) applied to
  * n rgb triples (stride 4 floats), written as n*3 floats. */
 void oracle_tonemap(const float* rgba, size_t n, float* out_rgb);

@@ -109,6 +109,9 @@ SIGNATURES = {
     "mm_context_destroy": (C.c_int, [C.c_void_p]),
     "mm_clouds_march": (C.c_int, [C.c_void_p, C.POINTER(Uniforms), C.POINTER(SceneTextures), C.POINTER(Image),
                                   C.POINTER(MarchOptions), C.c_void_p]),
+    "mm_clouds_reproject": (C.c_int, [C.c_void_p, C.POINTER(Uniforms), C.POINTER(Image), C.POINTER(Image), C.c_void_p]),
+    "mm_clouds_frame": (C.c_int, [C.c_void_p, C.POINTER(Uniforms), C.POINTER(SceneTextures), C.POINTER(Image),
+                                  C.POINTER(Image), C.POINTER(MarchOptions), C.c_void_p]),
     "mm_batch_options_default": (C.c_int, [C.POINTER(BatchOptions)]),
     "mm_clouds_march_batch": (C.c_int, [C.c_void_p, C.POINTER(View), C.c_int, C.POINTER(SceneTextures),
                                         C.POINTER(BatchOptions), C.c_void_p]),

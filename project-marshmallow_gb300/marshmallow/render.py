@@ -122,6 +122,23 @@ class Renderer:
         L.check(self.lib.mm_clouds_march(self.ctx, C.byref(u), C.byref(st), C.byref(img), C.byref(o),
                                          _stream_ptr(stream)), "mm_clouds_march")
 
+    @staticmethod
+    def image(rgba, depth=None):
+        h, w = rgba.shape[0], rgba.shape[1]
+        return L.Image(rgba.data_ptr(), rgba.stride(0) * 4, depth.data_ptr() if depth is not None else None,
+                       depth.stride(0) * 4 if depth is not None else 0, w, h)
+
+    def reproject(self, u, src, dst, stream=None):
+        """src, dst: (rgba, depth) tensor pairs of the same size."""
+        L.check(self.lib.mm_clouds_reproject(self.ctx, C.byref(u), C.byref(self.image(*src)), C.byref(self.image(*dst)),
+                                             _stream_ptr(stream)), "mm_clouds_reproject")
+
+    def frame(self, u, textures, prev, out, stream=None, **opts):
+        o = self.options(**opts)
+        st = textures.scene() if isinstance(textures, Textures) else textures
+        L.check(self.lib.mm_clouds_frame(self.ctx, C.byref(u), C.byref(st), C.byref(self.image(*prev)),
+                                         C.byref(self.image(*out)), C.byref(o), _stream_ptr(stream)), "mm_clouds_frame")
+
     def march_batch(self, views, textures, outputs, stream=None, warp_tile_w=8, tiles_per_grab=4, use_graph=1):
         """views: (width, height, uniforms) triples; outputs: matching (rgba, depth) CUDA tensors."""
         arr = (L.View * len(views))()

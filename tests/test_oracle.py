@@ -145,3 +145,29 @@ def test_oracle_horizon_rays_and_night(orc):
     tex["night_sky"] = night
     rgba, depth, _ = orc.march(un, tex, 48, 48)
     assert np.all(np.isfinite(rgba))
+
+
+def test_reprojection_static_camera_is_identity(orc):
+    # reproject.comp with camera == cameraPrev maps every pixel onto itself: the ten taps collapse
+    # onto the pixel, so the result is the source up to the rounding of the ten-tap average.
+    import marshmallow as mm
+    u = mm.scene.uniforms(96, 64, yaw=30.0, pitch=12.0)
+    rng = np.random.default_rng(4)
+    src = rng.uniform(0, 5, (64, 96, 4)).astype(np.float32)
+    dep = rng.uniform(1e3, 1e5, (64, 96)).astype(np.float32)
+    out, od = orc.reproject(u, src, dep)
+    assert np.allclose(out, src, rtol=2e-7, atol=0)
+    assert np.array_equal(out[..., 3], src[..., 3]) and np.array_equal(od, dep)
+
+
+def test_reprojection_follows_camera_motion(orc):
+    # Turning the camera right by a few degrees moves the previous image left in the new frame.
+    import marshmallow as mm
+    prev = mm.scene.uniforms(128, 64, yaw=20.0, pitch=15.0)
+    cur = mm.scene.uniforms(128, 64, yaw=23.0, pitch=15.0)
+    cur.camera_prev = prev.camera_prev
+    src = np.zeros((64, 128, 4), np.float32)
+    src[:, 60:68, :] = 1.0  # a bright vertical band at x = 60..67 in the previous frame
+    out, _ = orc.reproject(cur, src)
+    cols = np.where(out[32, :, 3] > 0.5)[0]
+    assert len(cols) > 0 and abs(cols.mean() - 63.5) > 2.0

@@ -302,6 +302,70 @@ int mm_clouds_frame(mm_context ctx, const mm_uniforms* u, const mm_scene_texture
                     const mm_image* out, const mm_march_options* opt, void* stream);
 
 /* ------------------------------------------------------------------------------------------ */
+/* Mesh cloud shadows: the low-res march of the mesh fragment shader (model.frag:52-130,       */
+/* 229-276), run over a G-buffer instead of rasterized fragments.                             */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Per pixel, the world position of the mesh fragment that covers it (model.vert:39,
+ * fragPositionWC): float4 rows, xyz the position, w != 0 where a fragment covers the pixel and 0
+ * where none does.  Device memory; pitch >= 16 * width and a multiple of 16. */
+typedef struct mm_gbuffer {
+    const float* world_pos;
+    size_t world_pos_pitch_bytes;
+    int width, height;
+} mm_gbuffer;
+
+/* For every covered pixel: six low-res density samples from the fragment towards the sun; the
+ * shadow is the largest density met (1 once above 0.99).  Writes it to `shadow` (float rows,
+ * 0 on uncovered pixels; may be NULL) and, if `rgba` (float4 rows holding the lit mesh colour,
+ * may be NULL) is given, darkens covered pixels in place to (max(rgb * (1 - 2 shadow), 0), 1) as
+ * the shader's last lines do (:275-277).  Reads tex->weather (the reference's cloudPlacement) and
+ * tex->low_res.  opt (NULL = defaults) supplies sampler, math and coverage_offset; its other fields
+ * are ignored.  Replaces the cloud-shadow part of the mesh draw (VulkanApplication.cpp:965). */
+int mm_mesh_shadow(mm_context ctx, const mm_uniforms* u, const mm_scene_textures* tex, const mm_gbuffer* gbuf,
+                   float* shadow, size_t shadow_pitch_bytes, float* rgba, size_t rgba_pitch_bytes,
+                   const mm_march_options* opt, void* stream);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Post chain: the reference's offscreen passes after the clouds (VulkanApplication.cpp:926-1010)  */
+/* as CUDA kernels on device buffers (no graphics API): god rays (god-ray.frag:41-76), radial      */
+/* blur (radialBlur.frag:112-139), the mesh over the blurred sky, Uncharted-2 tonemap + vignette  */
+/* (tonemap.frag:150-173) into the 8-bit swapchain layout.                                        */
+/* ------------------------------------------------------------------------------------------ */
+
+typedef struct mm_post_options {
+    int math; /* mm_math_mode: EXACT = the shaders' arithmetic (bit-reproducible), FAST = FMA + SFU pow */
+    int bgra; /* 1: bytes B,G,R,A as the B8G8R8A8_UNORM swapchain (VulkanApplication.cpp:1437-1446); 0: R,G,B,A */
+} mm_post_options;
+
+/* math FAST, bgra 1. */
+int mm_post_options_default(mm_post_options* o);
+
+/* Pixel (x, y) of every pass has fragUV = ((x + 0.5) / W, (y + 0.5) / H) (the full-screen quad of
+ * Geometry.cpp:91-101); a fetch at the fragment's own uv returns the texel, other taps are bilinear
+ * with CLAMP_TO_EDGE (the offscreen sampler, VulkanApplication.cpp:1290-1305).  Images are RGBA32F
+ * (mm_image; depth fields ignored); src and dst must not overlap.  With the sun below the horizon
+ * both passes copy the colour with alpha 1, as the shaders do. */
+
+/* god-ray.frag: dst = (src.rgb, god-ray term from eight taps of src.a towards the sun). */
+int mm_post_god_rays(mm_context ctx, const mm_uniforms* u, const mm_image* src, const mm_image* dst,
+                     const mm_post_options* opt, void* stream);
+/* radialBlur.frag: dst = (sun.color.rgb * sun.intensity * mean of ten taps of src.a * 1.1
+ * + 0.5 src.rgb, 1). */
+int mm_post_radial_blur(mm_context ctx, const mm_uniforms* u, const mm_image* src, const mm_image* dst,
+                        const mm_post_options* opt, void* stream);
+/* tonemap.frag: Uncharted-2 (exposure 0.7, white 50.2, gamma 1/2.2), vignette towards
+ * (0.1, 0.05, 0.13), UNORM8 (round to nearest even, alpha 255) into `out` (4 bytes per pixel). */
+int mm_post_tonemap(mm_context ctx, const mm_image* src, void* out, size_t out_pitch_bytes,
+                    const mm_post_options* opt, void* stream);
+/* The whole chain in two kernels: clouds -> god rays -> radial blur -> mesh layer (pixels with
+ * a != 0 replace the blurred sky, as the mesh draw after the blur does; may be NULL) -> tonemap
+ * -> 8 bits.  Equal to the four passes above run through RGBA32F framebuffers.  Keeps a float
+ * scratch plane of the frame size in the context. */
+int mm_post_chain(mm_context ctx, const mm_uniforms* u, const mm_image* clouds, const mm_image* mesh, void* out,
+                  size_t out_pitch_bytes, const mm_post_options* opt, void* stream);
+
+/* ------------------------------------------------------------------------------------------ */
 /* Many views in one launch.  No counterpart in the reference, which renders one camera.          */
 /* ------------------------------------------------------------------------------------------ */
 

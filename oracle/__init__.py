@@ -60,6 +60,14 @@ def load():
         lib.oracle_tonemap.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p]
         lib.oracle_reproject_f32.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
                                              C.c_void_p]
+        lib.oracle_shadow_f32.argtypes = [C.c_void_p, C.POINTER(OracleTextures), C.c_void_p, C.c_size_t, C.c_float,
+                                          C.c_void_p, C.c_int]
+        lib.oracle_shadow_f64.argtypes = lib.oracle_shadow_f32.argtypes
+        lib.oracle_post_god_rays.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+        lib.oracle_post_radial_blur.argtypes = lib.oracle_post_god_rays.argtypes
+        lib.oracle_post_tonemap.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_size_t, C.c_int]
+        lib.oracle_post_chain.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                          C.c_size_t, C.c_int]
         _lib = lib
     return _lib
 
@@ -117,6 +125,27 @@ def march(uniforms, textures, width, height, precision=32, pixel_mode=0, coverag
     return rgba, depth, cnt
 
 
+def _textures(textures):
+    keep = {k: np.ascontiguousarray(v) for k, v in textures.items() if v is not None}
+    t = OracleTextures(_tex(keep.get("weather")), _tex(keep.get("night_sky")), _tex(keep.get("curl")),
+                       _tex(keep.get("low_res")), _tex(keep.get("hi_res")))
+    return keep, t
+
+
+def shadow(uniforms, textures, world_pos, precision=32, coverage_offset=0.0, nthreads=0):
+    """model.frag's cloud-shadow march over a G-buffer of world positions (..., 4) -> shadow (...)."""
+    lib = load()
+    keep, t = _textures(textures)
+    pos = np.ascontiguousarray(world_pos, np.float32)
+    out = np.zeros(pos.shape[:-1], np.float32)
+    nth = nthreads or os.cpu_count() or 1
+    fn = lib.oracle_shadow_f32 if precision == 32 else lib.oracle_shadow_f64
+    rc = fn(C.addressof(uniforms), C.byref(t), pos.ctypes.data, pos.size // 4, coverage_offset, out.ctypes.data, nth)
+    if rc:
+        raise RuntimeError("oracle shadow failed: %d" % rc)
+    return out
+
+
 def tonemap(rgba):
     """tonemap.frag's Uncharted-2 operator on an (..., 4) float array -> (..., 3)."""
     a = np.ascontiguousarray(rgba, np.float32)
@@ -137,3 +166,32 @@ def reproject(uniforms, src_rgba, src_depth=None):
     if rc:
         raise RuntimeError("oracle reproject failed: %d" % rc)
     return out, od
+
+
+def post_pass(which, uniforms, src):
+    """One post pass on an (h, w, 4) float32 image: which = "god_rays" | "radial_blur"."""
+    a = np.ascontiguousarray(src, np.float32)
+    out = np.zeros_like(a)
+    fn = getattr(load(), "oracle_post_" + which)
+    if fn(C.addressof(uniforms), a.ctypes.data, a.shape[1], a.shape[0], out.ctypes.data):
+        raise RuntimeError("oracle post pass failed")
+    return out
+
+
+def post_tonemap(src, bgra=0):
+    a = np.ascontiguousarray(src, np.float32)
+    out = np.zeros(a.shape[:2] + (4,), np.uint8)
+    if load().oracle_post_tonemap(a.ctypes.data, a.shape[1], a.shape[0], out.ctypes.data, a.shape[1] * 4, bgra):
+        raise RuntimeError("oracle tonemap failed")
+    return out
+
+
+def post_chain(uniforms, clouds, mesh=None, bgra=0):
+    """clouds (and the optional mesh layer) (h, w, 4) float32 -> (h, w, 4) uint8."""
+    a = np.ascontiguousarray(clouds, np.float32)
+    m = np.ascontiguousarray(mesh, np.float32) if mesh is not None else None
+    out = np.zeros(a.shape[:2] + (4,), np.uint8)
+    if load().oracle_post_chain(C.addressof(uniforms), a.ctypes.data, m.ctypes.data if m is not None else None,
+                                a.shape[1], a.shape[0], out.ctypes.data, a.shape[1] * 4, bgra):
+        raise RuntimeError("oracle post chain failed")
+    return out

@@ -10,6 +10,9 @@
  *    samplers (LINEAR, REPEAT, normalized coordinates, mip 0; Texture.cpp:29-52, 315-338).
  *  - oracle_ref_curl: a restatement of SkyEngine/SkyEngine/ImageUtils.cpp:25-222
  *    (GenerateCurlNoise), pinned against the shipped Textures/CurlNoiseFBM.tga.
+ *  - oracle_shadow_*: the cloud-shadow march of the mesh pass, SkyEngine/SkyEngine/Shaders/model.frag.
+ *  - oracle_reproject_f32: the reprojection pass, SkyEngine/SkyEngine/Shaders/reproject.comp.
+ *  - oracle_post_*: the post chain (god rays, radial blur, tonemap) of the reference's offscreen passes.
  *  - oracle_noise_fill: the seeded Perlin-Worley / Worley / curl / weather generators that stand in
  *    for the pre-baked Nubis textures (which have no generator in the reference).
  */
@@ -74,6 +77,25 @@ uint32_t oracle_hash3(int32_t x, int32_t y, int32_t z, uint32_t s);
  * camera and camera_prev blocks of u.  Depth (new) follows the centre tap, as alpha does. */
 int oracle_reproject_f32(const mm_uniforms* u, const float* src_rgba, const float* src_depth, int w, int h,
                          float* dst_rgba, float* dst_depth);
+
+/* Cloud shadow of the mesh pass (model.frag:52-130, 229-276) for n G-buffer pixels: world_pos holds
+ * float4 (xyz world position, w != 0 where a mesh fragment covers the pixel); out_shadow gets the
+ * accumulated density (0 on uncovered pixels).  coverage_offset is added to weather.r, as in the march. */
+int oracle_shadow_f32(const mm_uniforms* u, const oracle_textures* t, const float* world_pos, size_t n,
+                      float coverage_offset, float* out_shadow, int nthreads);
+int oracle_shadow_f64(const mm_uniforms* u, const oracle_textures* t, const float* world_pos, size_t n,
+                      float coverage_offset, float* out_shadow, int nthreads);
+
+/* The post chain (god-ray.frag:41-76, radialBlur.frag:112-139, tonemap.frag:150-173) on w x h RGBA32F
+ * images (rows of 4 floats).  god_rays: dst = (src.rgb, god-ray term); radial_blur: dst =
+ * (sun colour * intensity * blur(src.a) + 0.5 src.rgb, 1); tonemap: 8-bit (bgra: B,G,R,A byte order
+ * as the B8G8R8A8 swapchain, else R,G,B,A; A = 255).  chain: clouds -> god rays -> radial blur ->
+ * mesh pixels (a != 0) drawn over it (mesh may be NULL) -> tonemap. */
+int oracle_post_god_rays(const mm_uniforms* u, const float* src, int w, int h, float* dst);
+int oracle_post_radial_blur(const mm_uniforms* u, const float* src, int w, int h, float* dst);
+int oracle_post_tonemap(const float* src, int w, int h, uint8_t* out, size_t pitch, int bgra);
+int oracle_post_chain(const mm_uniforms* u, const float* clouds, const float* mesh, int w, int h, uint8_t* out,
+                      size_t pitch, int bgra);
 
 /* Uncharted-2 tonemap of tonemap.frag:10-28 (exposure 0.7, white 50.2, gamma 1/2.2) applied to
  * n rgb triples (stride 4 floats), written as n*3 floats. */

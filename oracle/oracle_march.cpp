@@ -27,135 +27,9 @@
 #include <vector>
 
 #include "../project-marshmallow_gb300/csrc/mm_math.h"
-#include "oracle.h"
+#include "oracle_glsl.h"
 
 namespace {
-
-template <class T>
-struct Fn;
-
-template <>
-struct Fn<float> {
-    static float exp(float x) { return mmx::mm_expf(x); }
-    static float pow(float x, float y) { return mmx::mm_powf(x, y); }
-    static float acos(float x) { return mmx::mm_acosf(x); }
-    static float cos(float x) { return mmx::mm_cosf(x); }
-    static float sin(float x) { return mmx::mm_sinf(x); }
-    static float sqrt(float x) { return sqrtf(x); }
-    static float floor(float x) { return floorf(x); }
-    static float max(float a, float b) { return fmaxf(a, b); }
-    static float min(float a, float b) { return fminf(a, b); }
-};
-
-template <>
-struct Fn<double> {
-    static double exp(double x) { return ::exp(x); }
-    static double pow(double x, double y) { return ::pow(x, y); }
-    static double acos(double x) { return ::acos(x); }
-    static double cos(double x) { return ::cos(x); }
-    static double sin(double x) { return ::sin(x); }
-    static double sqrt(double x) { return ::sqrt(x); }
-    static double floor(double x) { return ::floor(x); }
-    static double max(double a, double b) { return fmax(a, b); }
-    static double min(double a, double b) { return fmin(a, b); }
-};
-
-template <class T>
-struct V3 {
-    T x, y, z;
-};
-template <class T>
-struct V4 {
-    T x, y, z, w;
-};
-
-template <class T> inline V3<T> operator+(V3<T> a, V3<T> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
-template <class T> inline V3<T> operator-(V3<T> a, V3<T> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
-template <class T> inline V3<T> operator*(V3<T> a, V3<T> b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
-template <class T> inline V3<T> operator/(V3<T> a, V3<T> b) { return {a.x / b.x, a.y / b.y, a.z / b.z}; }
-template <class T> inline V3<T> operator*(T s, V3<T> a) { return {s * a.x, s * a.y, s * a.z}; }
-template <class T> inline V3<T> operator*(V3<T> a, T s) { return {a.x * s, a.y * s, a.z * s}; }
-template <class T> inline V3<T> operator+(V3<T> a, T s) { return {a.x + s, a.y + s, a.z + s}; }
-template <class T> inline V3<T> operator-(T s, V3<T> a) { return {s - a.x, s - a.y, s - a.z}; }
-template <class T> inline V3<T> operator-(V3<T> a) { return {-a.x, -a.y, -a.z}; }
-template <class T> inline T dot(V3<T> a, V3<T> b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
-template <class T> inline T length(V3<T> a) { return Fn<T>::sqrt(dot(a, a)); }
-template <class T> inline V3<T> normalize(V3<T> a) { return a * (T(1) / Fn<T>::sqrt(dot(a, a))); }
-template <class T> inline T clampT(T x, T lo, T hi) { return Fn<T>::min(Fn<T>::max(x, lo), hi); }
-template <class T> inline T mixT(T x, T y, T a) { return x * (T(1) - a) + y * a; }
-template <class T> inline V3<T> mix3(V3<T> x, V3<T> y, T a) { return x * (T(1) - a) + y * a; }
-template <class T> inline V3<T> mix3v(V3<T> x, V3<T> y, V3<T> a) {
-    return {x.x * (T(1) - a.x) + y.x * a.x, x.y * (T(1) - a.y) + y.y * a.y, x.z * (T(1) - a.z) + y.z * a.z};
-}
-template <class T> inline T smoothstepT(T e0, T e1, T x) {
-    T t = clampT((x - e0) / (e1 - e0), T(0), T(1));
-    return t * t * (T(3) - T(2) * t);
-}
-template <class T> inline V3<T> pow3(V3<T> a, T e) {
-    return {Fn<T>::pow(a.x, e), Fn<T>::pow(a.y, e), Fn<T>::pow(a.z, e)};
-}
-template <class T> inline V3<T> exp3(V3<T> a) { return {Fn<T>::exp(a.x), Fn<T>::exp(a.y), Fn<T>::exp(a.z)}; }
-
-// mat3 stored as three columns
-template <class T>
-struct M3 {
-    V3<T> c[3];
-};
-template <class T> inline V3<T> mul(const M3<T>& m, V3<T> v) {
-    return {(m.c[0].x * v.x + m.c[1].x * v.y) + m.c[2].x * v.z,
-            (m.c[0].y * v.x + m.c[1].y * v.y) + m.c[2].y * v.z,
-            (m.c[0].z * v.x + m.c[1].z * v.y) + m.c[2].z * v.z};
-}
-
-// ---------------------------------------------------------------------------------- samplers
-
-inline int wrap(int i, int n) {
-    int m = i % n;
-    return m < 0 ? m + n : m;
-}
-
-template <class T>
-inline V4<T> fetch(const oracle_texture& t, int x, int y, int z) {
-    const uint8_t* p = t.texels + (((size_t)z * t.height + y) * t.width + x) * t.channels;
-    const T k = T(255);
-    switch (t.channels) {
-        case 4: return {(T)p[0] / k, (T)p[1] / k, (T)p[2] / k, (T)p[3] / k};
-        case 2: return {(T)p[0] / k, (T)p[1] / k, T(0), T(1)};
-        default: return {(T)p[0] / k, T(0), T(0), T(1)};
-    }
-}
-
-template <class T>
-inline V4<T> mix4(V4<T> a, V4<T> b, T w) {
-    return {mixT(a.x, b.x, w), mixT(a.y, b.y, w), mixT(a.z, b.z, w), mixT(a.w, b.w, w)};
-}
-
-template <class T>
-V4<T> sample2d(const oracle_texture& t, T u, T v) {
-    T x = u * (T)t.width - T(0.5), y = v * (T)t.height - T(0.5);
-    T fx = Fn<T>::floor(x), fy = Fn<T>::floor(y);
-    T ax = x - fx, ay = y - fy;
-    int x0 = wrap((int)fx, t.width), x1 = wrap((int)fx + 1, t.width);
-    int y0 = wrap((int)fy, t.height), y1 = wrap((int)fy + 1, t.height);
-    V4<T> a = mix4(fetch<T>(t, x0, y0, 0), fetch<T>(t, x1, y0, 0), ax);
-    V4<T> b = mix4(fetch<T>(t, x0, y1, 0), fetch<T>(t, x1, y1, 0), ax);
-    return mix4(a, b, ay);
-}
-
-template <class T>
-V4<T> sample3d(const oracle_texture& t, V3<T> p) {
-    T x = p.x * (T)t.width - T(0.5), y = p.y * (T)t.height - T(0.5), z = p.z * (T)t.depth - T(0.5);
-    T fx = Fn<T>::floor(x), fy = Fn<T>::floor(y), fz = Fn<T>::floor(z);
-    T ax = x - fx, ay = y - fy, az = z - fz;
-    int x0 = wrap((int)fx, t.width), x1 = wrap((int)fx + 1, t.width);
-    int y0 = wrap((int)fy, t.height), y1 = wrap((int)fy + 1, t.height);
-    int z0 = wrap((int)fz, t.depth), z1 = wrap((int)fz + 1, t.depth);
-    V4<T> a = mix4(fetch<T>(t, x0, y0, z0), fetch<T>(t, x1, y0, z0), ax);
-    V4<T> b = mix4(fetch<T>(t, x0, y1, z0), fetch<T>(t, x1, y1, z0), ax);
-    V4<T> d = mix4(fetch<T>(t, x0, y0, z1), fetch<T>(t, x1, y0, z1), ax);
-    V4<T> e = mix4(fetch<T>(t, x0, y1, z1), fetch<T>(t, x1, y1, z1), ax);
-    return mix4(mix4(a, b, ay), mix4(d, e, ay), az);
-}
 
 // ---------------------------------------------------------------------------------- the pass
 

@@ -340,6 +340,7 @@ int mm_context_destroy(mm_context c) {
     cudaFree(c->sur_meta);
     cudaFree(c->sur_y);
     cudaFree(c->sur_ray);
+    cudaFree(c->post_plane);
     delete c;
     return MM_OK;
 }

@@ -53,6 +53,8 @@ struct mm_context_s {
     void* sur_ray = nullptr;
     size_t sur_cap = 0, sur_pixels = 0;
     void* batch = nullptr;  // multi-view launch state (batch.cu)
+    float* post_plane = nullptr;  // god-ray term of the post chain (post.cu)
+    size_t post_plane_bytes = 0;
 };
 
 namespace mm {

@@ -78,6 +78,15 @@ class MarchOptions(C.Structure):
                 ("d_counters", C.c_void_p), ("schedule", C.c_int), ("cone", C.c_int), ("surrogate", C.c_void_p)]
 
 
+class GBuffer(C.Structure):
+    _fields_ = [("world_pos", C.c_void_p), ("world_pos_pitch_bytes", C.c_size_t), ("width", C.c_int),
+                ("height", C.c_int)]
+
+
+class PostOptions(C.Structure):
+    _fields_ = [("math", C.c_int), ("bgra", C.c_int)]
+
+
 class View(C.Structure):
     _fields_ = [("u", Uniforms), ("out", Image), ("coverage_offset", C.c_float)]
 
@@ -112,6 +121,18 @@ SIGNATURES = {
     "mm_clouds_reproject": (C.c_int, [C.c_void_p, C.POINTER(Uniforms), C.POINTER(Image), C.POINTER(Image), C.c_void_p]),
     "mm_clouds_frame": (C.c_int, [C.c_void_p, C.POINTER(Uniforms), C.POINTER(SceneTextures), C.POINTER(Image),
                                   C.POINTER(Image), C.POINTER(MarchOptions), C.c_void_p]),
+    "mm_mesh_shadow": (C.c_int, [C.c_void_p, C.POINTER(Uniforms), C.POINTER(SceneTextures), C.POINTER(GBuffer),
+                                 C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.POINTER(MarchOptions),
+                                 C.c_void_p]),
+    "mm_post_options_default": (C.c_int, [C.POINTER(PostOptions)]),
+    "mm_post_god_rays": (C.c_int, [C.c_void_p, C.POINTER(Uniforms), C.POINTER(Image), C.POINTER(Image),
+                                   C.POINTER(PostOptions), C.c_void_p]),
+    "mm_post_radial_blur": (C.c_int, [C.c_void_p, C.POINTER(Uniforms), C.POINTER(Image), C.POINTER(Image),
+                                      C.POINTER(PostOptions), C.c_void_p]),
+    "mm_post_tonemap": (C.c_int, [C.c_void_p, C.POINTER(Image), C.c_void_p, C.c_size_t, C.POINTER(PostOptions),
+                                  C.c_void_p]),
+    "mm_post_chain": (C.c_int, [C.c_void_p, C.POINTER(Uniforms), C.POINTER(Image), C.POINTER(Image), C.c_void_p,
+                                C.c_size_t, C.POINTER(PostOptions), C.c_void_p]),
     "mm_batch_options_default": (C.c_int, [C.POINTER(BatchOptions)]),
     "mm_clouds_march_batch": (C.c_int, [C.c_void_p, C.POINTER(View), C.c_int, C.POINTER(SceneTextures),
                                         C.POINTER(BatchOptions), C.c_void_p]),

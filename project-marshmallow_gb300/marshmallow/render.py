@@ -139,6 +139,49 @@ class Renderer:
         L.check(self.lib.mm_clouds_frame(self.ctx, C.byref(u), C.byref(st), C.byref(self.image(*prev)),
                                          C.byref(self.image(*out)), C.byref(o), _stream_ptr(stream)), "mm_clouds_frame")
 
+    def mesh_shadow(self, u, textures, world_pos, shadow=None, rgba=None, stream=None, **opts):
+        """model.frag's cloud-shadow march over a G-buffer: world_pos (H, W, 4) float32 CUDA tensor;
+        shadow (H, W) float32 and/or rgba (H, W, 4) float32 CUDA tensors receive the result."""
+        o = self.options(**opts)
+        st = textures.scene() if isinstance(textures, Textures) else textures
+        h, w = world_pos.shape[:2]
+        g = L.GBuffer(world_pos.data_ptr(), world_pos.stride(0) * 4, w, h)
+        L.check(self.lib.mm_mesh_shadow(self.ctx, C.byref(u), C.byref(st), C.byref(g),
+                                        shadow.data_ptr() if shadow is not None else None,
+                                        shadow.stride(0) * 4 if shadow is not None else 0,
+                                        rgba.data_ptr() if rgba is not None else None,
+                                        rgba.stride(0) * 4 if rgba is not None else 0, C.byref(o),
+                                        _stream_ptr(stream)), "mm_mesh_shadow")
+
+    @staticmethod
+    def post_options(math=L.MATH_FAST, bgra=1):
+        return L.PostOptions(math, bgra)
+
+    @staticmethod
+    def _rgba_image(t):
+        return L.Image(t.data_ptr(), t.stride(0) * 4, None, 0, t.shape[1], t.shape[0])
+
+    def god_rays(self, u, src, dst, stream=None, **opts):
+        L.check(self.lib.mm_post_god_rays(self.ctx, C.byref(u), C.byref(self._rgba_image(src)),
+                                          C.byref(self._rgba_image(dst)), C.byref(self.post_options(**opts)),
+                                          _stream_ptr(stream)), "mm_post_god_rays")
+
+    def radial_blur(self, u, src, dst, stream=None, **opts):
+        L.check(self.lib.mm_post_radial_blur(self.ctx, C.byref(u), C.byref(self._rgba_image(src)),
+                                             C.byref(self._rgba_image(dst)), C.byref(self.post_options(**opts)),
+                                             _stream_ptr(stream)), "mm_post_radial_blur")
+
+    def tonemap(self, src, out8, stream=None, **opts):
+        """src (H, W, 4) float32, out8 (H, W, 4) uint8 CUDA tensors."""
+        L.check(self.lib.mm_post_tonemap(self.ctx, C.byref(self._rgba_image(src)), out8.data_ptr(), out8.stride(0),
+                                         C.byref(self.post_options(**opts)), _stream_ptr(stream)), "mm_post_tonemap")
+
+    def post_chain(self, u, clouds, out8, mesh=None, stream=None, **opts):
+        m = C.byref(self._rgba_image(mesh)) if mesh is not None else None
+        L.check(self.lib.mm_post_chain(self.ctx, C.byref(u), C.byref(self._rgba_image(clouds)), m, out8.data_ptr(),
+                                       out8.stride(0), C.byref(self.post_options(**opts)), _stream_ptr(stream)),
+                "mm_post_chain")
+
     def march_batch(self, views, textures, outputs, stream=None, warp_tile_w=8, tiles_per_grab=4, use_graph=1):
         """views: (width, height, uniforms) triples; outputs: matching (rgba, depth) CUDA tensors."""
         arr = (L.View * len(views))()

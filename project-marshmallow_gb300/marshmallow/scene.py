@@ -54,3 +54,64 @@ def batch_views(seed=0):
         views.append((3840, 2160, uniforms(3840, 2160, yaw=rng.uniform(0.0, 360.0), pitch=rng.uniform(5.0, 25.0),
                                            time=rng.uniform(0.0, 2.0), sun_elevation=rng.uniform(5.0, 85.0))))
     return views
+
+
+def _camera_rays(u, width, height):
+    """Unit ray directions of every pixel, (height, width, 3) float64, as the march forms them
+    (compute-clouds.comp:309-322): p = (cam - look) + aspect * sx * tanHalfFov * right
+    - sy * tanHalfFov * up, rd = normalize(p - cam), sx, sy = 2 * pixel / size - 1."""
+    import numpy as np
+    v = np.array(u.camera.view[:], np.float64)
+    look, right, up = v[[2, 6, 10]], v[[0, 4, 8]], v[[1, 5, 9]]
+    aspect, tan = float(u.camera.camera_params[0]), float(u.camera.camera_params[1])
+    sx = 2.0 * np.arange(width, dtype=np.float64) / width - 1.0
+    sy = 2.0 * np.arange(height, dtype=np.float64) / height - 1.0
+    d = (-look)[None, None, :] + (aspect * tan) * sx[None, :, None] * right - tan * sy[:, None, None] * up
+    return d / np.linalg.norm(d, axis=-1, keepdims=True)
+
+
+def terrain_height(x, z, amplitude=40.0):
+    import numpy as np
+    return amplitude * (0.6 * np.sin(x / 310.0) * np.cos(z / 260.0) + 0.4 * np.sin((x + 2.0 * z) / 95.0))
+
+
+def terrain_gbuffer(u, width, height, amplitude=40.0, coarse_steps=48, refine_steps=30):
+    """A headless G-buffer for the mesh pass: the world position (model.vert's fragPositionWC) where
+    each pixel's camera ray first meets the height field y = terrain_height(x, z), as float4 rows
+    (height, width, 4) float32 with w = 1 where the ray hits the ground and 0 where it does not.
+    The first crossing is found by a coarse march between the planes y = +-amplitude and refined by
+    bisection."""
+    import numpy as np
+    rd = _camera_rays(u, width, height).reshape(-1, 3)
+    eye = np.array(u.camera.camera_position[:3], np.float64)
+    out = np.zeros((rd.shape[0], 4), np.float32)
+    down = rd[:, 1] < -1e-6
+    r = rd[down]
+    t0 = np.maximum(0.0, (eye[1] - amplitude) / -r[:, 1])
+    t1 = (eye[1] + amplitude) / -r[:, 1]
+
+    def g(t):
+        p = eye[None, :] + t[:, None] * r
+        return p[:, 1] - terrain_height(p[:, 0], p[:, 2], amplitude)
+
+    lo, hi = t0.copy(), t1.copy()
+    found = np.zeros(len(r), bool)
+    prev_t, prev_g = t0, g(t0)
+    for k in range(1, coarse_steps + 1):
+        t = t0 + (t1 - t0) * (k / coarse_steps)
+        gt = g(t)
+        hit = (~found) & (prev_g > 0) & (gt <= 0)
+        lo[hit], hi[hit] = prev_t[hit], t[hit]
+        found |= hit
+        prev_t, prev_g = t, gt
+    found &= g(t0) > 0
+    for _ in range(refine_steps):
+        mid = 0.5 * (lo + hi)
+        above = g(mid) > 0
+        lo = np.where(above, mid, lo)
+        hi = np.where(above, hi, mid)
+    p = eye[None, :] + hi[:, None] * r
+    sel = np.flatnonzero(down)[found]
+    out[sel, :3] = p[found]
+    out[sel, 3] = 1.0
+    return out.reshape(height, width, 4)

@@ -171,3 +171,82 @@ def test_reprojection_follows_camera_motion(orc):
     out, _ = orc.reproject(cur, src)
     cols = np.where(out[32, :, 3] > 0.5)[0]
     assert len(cols) > 0 and abs(cols.mean() - 63.5) > 2.0
+
+
+def _shadow_scene(orc, w=160, h=90, **kw):
+    import marshmallow as mm
+    import marshmallow.lib as L
+    u = mm.scene.uniforms(w, h, eye=(0.0, 150.0, 0.0), pitch=-20.0, **kw)
+    g = mm.scene.terrain_gbuffer(u, w, h)
+    tex = {"low_res": orc.noise(L.NOISE_LOWRES, 0, 64, 64, 64, 4), "weather": orc.noise(L.NOISE_WEATHER, 0, 256, 256, 1, 4)[0]}
+    return u, g, tex
+
+
+def test_shadow_f32_vs_f64_and_uncovered_pixels(orc):
+    # model.frag's shadow march: FP32 within 1e-4 of FP64 (a max of six densities, no accumulation);
+    # pixels without a mesh fragment get 0.
+    u, g, tex = _shadow_scene(orc, sun_elevation=45.0, time=5.0)
+    a = orc.shadow(u, tex, g)
+    b = orc.shadow(u, tex, g, precision=64)
+    cov = g[..., 3] != 0
+    assert 0.3 < cov.mean() < 1.0
+    assert np.all(a[~cov] == 0) and (a[cov] > 0).mean() > 0.2
+    assert np.all((a >= 0) & (a <= 1))
+    assert np.percentile(np.abs(a - b), 99.9) <= 1e-4
+    # multithreaded == single-threaded
+    assert np.array_equal(orc.shadow(u, tex, g, nthreads=1), a)
+
+
+def test_shadow_saturates_and_vanishes(orc):
+    # Empty low-res noise: no density anywhere.  Dense noise with a stratocumulus weather map: on
+    # almost every fragment a sample lands inside the layer and saturates the shadow to exactly 1
+    # (:266-269).
+    u, g, tex = _shadow_scene(orc, sun_elevation=60.0)
+    empty = dict(tex, low_res=np.zeros_like(tex["low_res"]))
+    assert np.all(orc.shadow(u, empty, g) == 0)
+    dense = np.full_like(tex["low_res"], 255)
+    dense[..., 1:] = 0
+    weather = np.zeros_like(tex["weather"])
+    weather[..., 2] = 128
+    s = orc.shadow(u, {"low_res": dense, "weather": weather}, g)
+    cov = g[..., 3] != 0
+    assert np.all((s >= 0) & (s <= 1)) and (s[cov] == 1.0).mean() > 0.9 and np.all(s[~cov] == 0)
+
+
+def test_post_chain_known_answers(orc):
+    # Uniform alpha a: each god-ray tap reads a, so the term is 0.9 * 0.5 a (1 + 0.125 sum 0.99^i)
+    # (god-ray.frag:56-75); the radial blur of a uniform term t is 1.1 t (radialBlur.frag:133-136).
+    import marshmallow as mm
+    u = mm.scene.uniforms(96, 64, yaw=0.0, pitch=15.0, sun_elevation=20.0)
+    img = np.zeros((64, 96, 4), np.float32)
+    img[..., :3] = np.random.default_rng(1).uniform(0, 1, (64, 96, 3))
+    img[..., 3] = 0.25
+    g = orc.post_pass("god_rays", u, img)
+    want = 0.9 * 0.5 * 0.25 * (1 + 0.125 * sum(0.99 ** i for i in range(8)))
+    assert np.allclose(g[..., 3], want, rtol=1e-6) and np.array_equal(g[..., :3], img[..., :3])
+    r = orc.post_pass("radial_blur", u, g)
+    k = np.array(u.sun.color[:3], np.float64) * u.sun.intensity
+    assert np.allclose(r[..., :3], k * 1.1 * want + 0.5 * img[..., :3], rtol=1e-5)
+    assert np.all(r[..., 3] == 1.0)
+    # The chain is the passes in sequence; a mesh layer replaces the blurred sky where its a != 0.
+    mesh = np.zeros_like(img)
+    mesh[40:, :, :3] = 0.3
+    mesh[40:, :, 3] = 1.0
+    out = orc.post_chain(u, img, mesh)
+    fb2 = r.copy()
+    fb2[40:] = mesh[40:]
+    assert np.array_equal(out, orc.post_tonemap(fb2))
+    # tonemap: B,G,R,A byte order by default is a channel swap of R,G,B,A; alpha 255.
+    t_rgba, t_bgra = orc.post_tonemap(fb2, bgra=0), orc.post_tonemap(fb2, bgra=1)
+    assert np.array_equal(t_rgba[..., [2, 1, 0, 3]], t_bgra) and np.all(t_rgba[..., 3] == 255)
+    # At the image centre the vignette vanishes: the 8-bit tonemap equals the FP64 metric tonemap.
+    c = orc.tonemap(fb2[31:33, 47:49])
+    assert np.max(np.abs(t_rgba[31:33, 47:49, :3].astype(int) - np.round(np.clip(c, 0, 1) * 255))) <= 1
+
+
+def test_post_chain_night_skips_the_sun_passes(orc):
+    # Sun below the horizon: both passes copy the colour (god-ray.frag:52-54, radialBlur.frag:117-119).
+    import marshmallow as mm
+    u = mm.scene.uniforms(64, 48, sun_elevation=-10.0)
+    img = np.random.default_rng(2).uniform(0, 3, (48, 64, 4)).astype(np.float32)
+    assert np.array_equal(orc.post_chain(u, img), orc.post_tonemap(img))

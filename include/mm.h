@@ -182,6 +182,27 @@ int mm_ref_curl_hash(const float* d_xyz, size_t n, float* d_out, void* stream);
 int mm_texture_create(const void* texels, int src_is_device, int width, int height, int depth,
                       int channels, int format, mm_texture* out, void* stream);
 
+/* Shipped assets (Texture::initFromFile / Texture3D::initFromFile, Texture.cpp:212-246, 502-538, with
+ * stb_image's stbi_load(..., STBI_rgb_alpha)).  Decodes TGA (uncompressed or RLE; 8-bit grey,
+ * 24/32-bit; either row order) and PNG (8- or 16-bit grey, grey+alpha, RGB, RGBA; not interlaced)
+ * to RGBA8 rows top to bottom as stbi_load does: grey g -> (g, g, g, 255), missing alpha -> 255,
+ * 16-bit samples -> their high byte, TGA rows flipped unless the descriptor has the top-left
+ * origin bit.  Other variants (palettes, interlacing, 16-bit TGA) return MM_ERR_UNSUPPORTED. */
+
+/* Decodes one file into a malloc'ed RGBA8 buffer (release with mm_image_free). */
+int mm_image_decode_file(const char* path, uint8_t** rgba, int* width, int* height);
+int mm_image_free(uint8_t* rgba);
+
+/* Texture::initFromFile: one image file -> a 2D RGBA texture (e.g. Textures/CloudPlacement.png
+ * for the weather map, NightSky/nightSky.png, CurlNoiseFBM.tga). */
+int mm_texture_load_file(const char* path, int format, mm_texture* out, void* stream);
+
+/* Texture3D::initFromFile: `depth` slices named prefix + "(" + i + ").tga", i = 0..depth-1
+ * (Texture.cpp:511; the reference passes ".../lowResCloudShape/lowResCloud" with depth 128 and
+ * ".../hiResCloudShape/hiResClouds " with depth 32, VulkanApplication.cpp:259-262) -> a 3D RGBA
+ * texture, slice i at z = i. */
+int mm_texture_load_slices(const char* prefix, int depth, int format, mm_texture* out, void* stream);
+
 /* Width/height/depth/channels/format of a texture. */
 int mm_texture_info(mm_texture tex, int* width, int* height, int* depth, int* channels,
                     int* format);

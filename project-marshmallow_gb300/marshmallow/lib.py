@@ -109,6 +109,10 @@ SIGNATURES = {
     "mm_ref_curl_hash": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]),
     "mm_texture_create": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                     C.POINTER(C.c_void_p), C.c_void_p]),
+    "mm_image_decode_file": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "mm_image_free": (C.c_int, [C.c_void_p]),
+    "mm_texture_load_file": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_void_p), C.c_void_p]),
+    "mm_texture_load_slices": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.POINTER(C.c_void_p), C.c_void_p]),
     "mm_texture_info": (C.c_int, [C.c_void_p] + [C.POINTER(C.c_int)] * 5),
     "mm_texture_copy_to_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "mm_texture_set_format": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),

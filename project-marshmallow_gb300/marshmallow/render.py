@@ -62,6 +62,34 @@ class Textures:
             handles[name] = hnd
         return cls(handles=handles)
 
+    # The files VulkanApplication.cpp:253-262 loads, relative to the reference's Textures/ folder.
+    ASSET_FILES = {
+        "weather": ("file", "CloudPlacement.png"),
+        "night_sky": ("file", "NightSky/nightSky_noOrange.png"),
+        "curl": ("file", "CurlNoiseFBM.png"),
+        "low_res": ("slices", "3DTextures/lowResCloudShape/lowResCloud", 128),
+        "hi_res": ("slices", "3DTextures/hiResCloudShape/hiResClouds ", 32),
+    }
+
+    @classmethod
+    def from_assets(cls, root, stream=None, fmt=L.FORMAT_UNORM8, files=None):
+        """The shipped Nubis texture set (or `files`, same layout) loaded by mm_texture_load_file /
+        mm_texture_load_slices from the folder `root`."""
+        import os
+        lib = L.load()
+        s = _stream_ptr(stream)
+        handles = {}
+        for name, spec in (files or cls.ASSET_FILES).items():
+            hnd = C.c_void_p()
+            path = os.path.join(root, spec[1]).encode()
+            if spec[0] == "file":
+                L.check(lib.mm_texture_load_file(path, fmt, C.byref(hnd), s), "mm_texture_load_file(%s)" % name)
+            else:
+                L.check(lib.mm_texture_load_slices(path, spec[2], fmt, C.byref(hnd), s),
+                        "mm_texture_load_slices(%s)" % name)
+            handles[name] = hnd
+        return cls(handles=handles)
+
     def host(self, name):
         lib = L.load()
         w, h, d, c, f = (C.c_int() for _ in range(5))

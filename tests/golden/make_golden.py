@@ -9,8 +9,12 @@
                       setTime (SkyManager.cpp, compiled by `make -C oracle ref`).
   nubis_stats.json    mean / deviation of the shipped Nubis density textures (the targets of the
                       seeded generators' output maps).
+  asset_digests.json  SHA-256 of the RGBA8 decode (stbi_load(..., STBI_rgb_alpha) conventions) of the
+                      shipped textures the reference loads, from the independent decoders in
+                      tests/tga.py and tests/png.py; the library's loader must reproduce them.
 
-Usage: python tests/golden/make_golden.py [REFERENCE_ROOT]
+Usage: python tests/golden/make_golden.py [REFERENCE_ROOT] [--digests-only]
+
 """
 import json
 import os
@@ -22,12 +26,53 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(REPO, "tests"))
+from png import read_png  # noqa: E402
 from tga import read_tga  # noqa: E402
+
+# Files VulkanApplication.cpp:253-262 loads (plus the TGA twin of the curl map), relative to Textures/.
+ASSETS = ["CloudPlacement.png", "NightSky/nightSky_noOrange.png", "CurlNoiseFBM.png", "CurlNoiseFBM.tga",
+          "3DTextures/lowResCloudShape/lowResCloud(0).tga", "3DTextures/lowResCloudShape/lowResCloud(77).tga",
+          "3DTextures/hiResCloudShape/hiResClouds (0).tga", "3DTextures/hiResCloudShape/hiResClouds (31).tga"]
+
+
+def rgba8(a, depth16=False):
+    """stbi_load(..., STBI_rgb_alpha) conversion of decoded samples (h, w, c)."""
+    if depth16:
+        a = a >> 8
+    a = a.astype(np.uint8)
+    h, w, c = a.shape
+    out = np.full((h, w, 4), 255, np.uint8)
+    if c <= 2:
+        out[..., :3] = a[..., :1]
+        if c == 2:
+            out[..., 3] = a[..., 1]
+    else:
+        out[..., :c] = a
+    return out
+
+
+def asset_digests(se):
+    import hashlib
+    d = {}
+    for name in ASSETS:
+        path = os.path.join(se, "Textures", name)
+        if name.endswith(".png"):
+            a = read_png(path)
+            img = rgba8(a, a.dtype == np.uint16)
+        else:
+            img = rgba8(read_tga(path))
+        d[name] = hashlib.sha256(img.tobytes()).hexdigest()
+    with open(os.path.join(HERE, "asset_digests.json"), "w") as f:
+        json.dump(d, f, indent=1)
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    ref = args[0] if args else "/root/reference"
     se = os.path.join(ref, "SkyEngine", "SkyEngine")
+    asset_digests(se)
+    if "--digests-only" in sys.argv:
+        return
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", "REF=" + ref], check=True)
     bins = os.path.join(REPO, "oracle", "_ref")
 

@@ -48,6 +48,7 @@ def parse_args():
     ap.add_argument("--math", choices=["fast", "exact"], default="fast")
     ap.add_argument("--schedule", choices=["persistent", "tiled"], default="tiled")
     ap.add_argument("--density", choices=["unorm8", "fp16"], default="unorm8")
+    ap.add_argument("--no-passes", action="store_true", help="skip the timings of the other passes")
     return ap.parse_args()
 
 
@@ -175,6 +176,120 @@ def run_reference(args):
         "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------------------ the other passes
+
+
+def _median_ms(fn, flush, stream, n=10, warm=3):
+    import torch
+    ts = []
+    for i in range(warm + n):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        if i >= warm:
+            ts.append(a.elapsed_time(b))
+    ts.sort()
+    return ts[len(ts) // 2]
+
+
+def _pass_line(ms, w, h, bytes_px, hbm_peak, note, cpu=None):
+    gbs = bytes_px * w * h / (ms * 1e-3) / 1e9
+    d = {"ms": round(ms, 4), "mpix_per_s": round(w * h / (ms * 1e-3) / 1e6, 1),
+         "algorithmic_bytes_per_pixel": bytes_px, "achieved_gbs": round(gbs, 1),
+         "hbm_frac": round(gbs / hbm_peak, 4) if hbm_peak else None, "note": note}
+    if cpu:
+        d["cpu_baseline"] = cpu
+    return d
+
+
+def _cpu_rate(fn, pixels):
+    t0 = time.perf_counter()
+    fn()
+    dt = time.perf_counter() - t0
+    return pixels / dt / 1e6, dt
+
+
+def measure_passes(renderer, textures, rgba, depth, uniforms, w, h, flush, stream, hbm_peak, with_cpu):
+    """Timings of the reference's other per-frame passes at the benchmark size (CUDA events, L2 flushed
+    before each launch, median of 10): reprojection, the 16-phase frame (reprojection + 1/16 march),
+    the mesh cloud-shadow march over a terrain G-buffer, the post chain to 8 bits; with CPU-oracle
+    rates on a 960x540 sample when with_cpu."""
+    import numpy as np
+    import torch
+    import marshmallow as mm
+    out = {}
+    src = (rgba, depth)
+    dst = (torch.empty_like(rgba), torch.empty_like(depth))
+    # Reprojection: motion of one sweep step (6 degrees of yaw) and of a 0.5 degree pan.
+    u_sweep = mm.scene.sweep_uniforms(5, w, h, n=SWEEP)
+    u_sweep.camera_prev = uniforms[4].camera_prev
+    p = sweep(5)
+    u_pan = mm.scene.uniforms(w, h, yaw=p["yaw"], pitch=p["pitch"], time=p["time"])
+    u_pan.camera_prev = mm.scene.uniforms(w, h, yaw=p["yaw"] - 0.5, pitch=p["pitch"], time=p["time"]).camera_prev
+    cpu = None
+    sw, sh = 960, 540
+    if with_cpu:
+        import oracle
+        us = mm.scene.sweep_uniforms(5, sw, sh, n=SWEEP)
+        us.camera_prev = mm.scene.sweep_uniforms(4, sw, sh, n=SWEEP).camera_prev
+        img = np.random.default_rng(0).uniform(0, 1, (sh, sw, 4)).astype(np.float32)
+        rate, dt = _cpu_rate(lambda: oracle.reproject(us, img, img[..., 0].copy()), sw * sh)
+        cpu = {"value": round(rate, 2), "unit": "Mpix/s", "cores": 1, "kind": "port",
+               "sample": "oracle reprojection of one %dx%d frame (%.2f s)" % (sw, sh, dt)}
+    out["reproject_sweep_step"] = _pass_line(
+        _median_ms(lambda: renderer.reproject(u_sweep, src, dst), flush, stream), w, h, 40.0, hbm_peak,
+        "reproject.comp, every pixel, motion of one sweep step (6 deg yaw); RGBA32F + depth in and out", cpu)
+    out["reproject_pan_0p5deg"] = _pass_line(
+        _median_ms(lambda: renderer.reproject(u_pan, src, dst), flush, stream), w, h, 40.0, hbm_peak,
+        "reproject.comp, every pixel, a 0.5 deg pan")
+    # The reference's per-frame compute work: reprojection + march of one pixel in 16.
+    u_f = mm.scene.sweep_uniforms(5, w, h, n=SWEEP, )
+    u_f.camera_prev = uniforms[4].camera_prev
+    u_f.sun.color[3] = 5.0
+    out["frame_phase16"] = _pass_line(
+        _median_ms(lambda: renderer.frame(u_f, textures, src, dst), flush, stream), w, h, 40.0, hbm_peak,
+        "mm_clouds_frame: reprojection of every pixel + march of the pixels of phase 5 (1/16)")
+    # Mesh cloud shadows over a terrain G-buffer (camera 150 m up, 20 deg down, sun 45 deg).
+    u_s = mm.scene.uniforms(w, h, eye=(0.0, 150.0, 0.0), pitch=-20.0, sun_elevation=45.0, time=5.0)
+    gbuf = mm.scene.terrain_gbuffer_cuda(u_s, w, h)
+    shadow = torch.empty((h, w), dtype=torch.float32, device="cuda")
+    cpu = None
+    if with_cpu:
+        import oracle
+        us = mm.scene.uniforms(sw, sh, eye=(0.0, 150.0, 0.0), pitch=-20.0, sun_elevation=45.0, time=5.0)
+        g = mm.scene.terrain_gbuffer(us, sw, sh)
+        host = {"weather": textures.host("weather"), "low_res": textures.host("low_res")}
+        threads = os.cpu_count() or 1
+        rate, dt = _cpu_rate(lambda: oracle.shadow(us, host, g, nthreads=threads), sw * sh)
+        cpu = {"value": round(rate, 2), "unit": "Mpix/s", "cores": threads, "kind": "port",
+               "sample": "oracle shadow march of one %dx%d terrain G-buffer (%.2f s)" % (sw, sh, dt)}
+    out["mesh_shadow"] = _pass_line(
+        _median_ms(lambda: renderer.mesh_shadow(u_s, textures, gbuf, shadow=shadow), flush, stream), w, h, 20.0,
+        hbm_peak, "model.frag cloud-shadow march, %.0f%% of pixels covered; float4 positions in, float shadow out"
+        % (100.0 * float((gbuf[..., 3] != 0).float().mean())), cpu)
+    del gbuf
+    # Post chain: god rays + radial blur + tonemap of a cloud frame looking at the sun -> 8 bits.
+    u_p = mm.scene.uniforms(w, h, yaw=0.0, pitch=12.0, sun_elevation=20.0)
+    renderer.march(u_p, textures, rgba)
+    out8 = torch.empty((h, w, 4), dtype=torch.uint8, device="cuda")
+    cpu = None
+    if with_cpu:
+        import oracle
+        up = mm.scene.uniforms(sw, sh, yaw=0.0, pitch=12.0, sun_elevation=20.0)
+        img = torch.nn.functional.interpolate(rgba.permute(2, 0, 1)[None], size=(sh, sw)).squeeze(0).permute(1, 2, 0)
+        img = img.contiguous().cpu().numpy()
+        rate, dt = _cpu_rate(lambda: oracle.post_chain(up, img), sw * sh)
+        cpu = {"value": round(rate, 2), "unit": "Mpix/s", "cores": 1, "kind": "port",
+               "sample": "oracle post chain of one %dx%d frame (%.2f s)" % (sw, sh, dt)}
+    out["post_chain"] = _pass_line(
+        _median_ms(lambda: renderer.post_chain(u_p, rgba, out8), flush, stream), w, h, 20.0, hbm_peak,
+        "god rays + radial blur + tonemap (two kernels); RGBA32F in, B8G8R8A8 out", cpu)
+    return out
 
 
 # ------------------------------------------------------------------------------ our arm
@@ -343,6 +458,11 @@ def run_ours(args):
                "sample": "FP32 oracle restatement of compute-clouds.comp on frames 0 and 8 of the sweep, every "
                          "4th row and column (%d rays, %.1f s)" % (rays, secs)}
 
+    passes = None
+    if rank == 0 and not args.no_passes:
+        passes = measure_passes(renderer, textures, rgba, depth, uniforms, w, h, flush, stream, hbm_peak,
+                                world == 1 and not args.no_cpu_baseline)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
@@ -370,6 +490,7 @@ def run_ours(args):
             "work_per_frame": {"cloud_test": n_test / args.steps, "cloud_hires": n_hires / args.steps,
                                "iterations": n_iter / args.steps, "accumulated": n_acc / args.steps},
             "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks, "cpu_baseline": cpu,
+            "passes": passes,
         }
         print(json.dumps(line), flush=True)
     renderer.close()

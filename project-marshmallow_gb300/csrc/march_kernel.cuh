@@ -717,8 +717,9 @@ __global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_MARCH_MIN_BLOCKS) marc
     cone_offsets(p.u, s_cone);
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int by = (int)blockIdx.y < p.row_split ? p.row_split - 1 - (int)blockIdx.y : (int)blockIdx.y;
     const int tx = blockIdx.x * kBlockTileW + (warp % (kBlockTileW / 8)) * 8 + (lane & 7);
-    const int ty = blockIdx.y * kBlockTileH + (warp / (kBlockTileW / 8)) * 4 + (lane >> 3);
+    const int ty = by * kBlockTileH + (warp / (kBlockTileW / 8)) * 4 + (lane >> 3);
     int px, py;
     if (p.pixel_mode == MM_PIXELS_PHASE16) {  // :292-298 (thread grid covers ceil(W/4) x ceil(H/4))
         px = tx * 4 + (p.phase % 4);
@@ -734,14 +735,42 @@ __global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_MARCH_MIN_BLOCKS) marc
     if (C) flush_work(p.counters, w);
 }
 
+// Launch order of the block rows.  A ray's cost grows as it nears the horizon (it crosses more of
+// the cloud shell: ~124 km at rd.y = 0 against 20 km straight up) and rays below it end at once,
+// so the rows just above the horizon are the long ones.  Started last, they would form the tail of
+// the launch (at 1/16 of a frame, a launch is only a few waves of rays).  For a camera without roll
+// (right.y == 0, as mm_camera_from_angles makes) the ray's y component depends on the row only and
+// falls monotonically down the image; the block rows whose centre ray rises are [0, split), and the
+// kernel runs them from split - 1 (the horizon) upwards before the rest.  Any other camera keeps
+// the launch order.  Only the order changes: every pixel is marched by the same code.
+inline int horizon_row_split(const MarchLaunch& p, int block_rows) {
+    const float* v = p.u.camera.view;
+    if (v[4] != 0.0f) return 0;
+    const float cpy = p.u.camera.camera_params[1];
+    const bool phase16 = p.pixel_mode == MM_PIXELS_PHASE16;
+    int split = 0;
+    for (int r = 0; r < block_rows; ++r) {
+        const int row = r * kBlockTileH + kBlockTileH / 2;
+        const int py = phase16 ? row * 4 + p.phase / 4 : row;
+        const float spy = 2.0f * (float)py / p.uv_h - 1.0f;
+        if (-v[6] - spy * cpy * v[5] > 0.0f)
+            split = r + 1;
+        else
+            break;
+    }
+    return split;
+}
+
 template <bool E, int S>
-int launch_tiled(const MarchLaunch& p, cudaStream_t s) {
+int launch_tiled(const MarchLaunch& p0, cudaStream_t s) {
+    MarchLaunch p = p0;
     int gw = p.width, gh = p.height;
     if (p.pixel_mode == MM_PIXELS_PHASE16) {
         gw = (p.width + 3) / 4;
         gh = (p.height + 3) / 4;
     }
     dim3 grid((gw + kBlockTileW - 1) / kBlockTileW, (gh + kBlockTileH - 1) / kBlockTileH);
+    p.row_split = horizon_row_split(p, (int)grid.y);
     if (p.counters)
         march_tiled_kernel<E, S, true><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
     else

@@ -79,6 +79,7 @@ struct MarchLaunch {
     float uv_w, uv_h;
     float coverage_offset;
     unsigned long long* counters;
+    int row_split;  // tiled march: block rows [0, row_split) run in reverse order first (0 = launch order)
 };
 
 // Kernel launchers (one translation unit per arithmetic mode).

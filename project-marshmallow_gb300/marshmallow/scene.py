@@ -115,3 +115,54 @@ def terrain_gbuffer(u, width, height, amplitude=40.0, coarse_steps=48, refine_st
     out[sel, :3] = p[found]
     out[sel, 3] = 1.0
     return out.reshape(height, width, 4)
+
+
+def terrain_gbuffer_cuda(u, width, height, amplitude=40.0, coarse_steps=48, refine_steps=30):
+    """terrain_gbuffer computed on the current CUDA device with torch (float64): returns an
+    (height, width, 4) float32 CUDA tensor.  Used to build large G-buffers quickly."""
+    import torch
+    dev = torch.device("cuda")
+    f64 = torch.float64
+    v = torch.tensor(list(u.camera.view), dtype=f64, device=dev)
+    look, right, up = v[[2, 6, 10]], v[[0, 4, 8]], v[[1, 5, 9]]
+    aspect, tan = float(u.camera.camera_params[0]), float(u.camera.camera_params[1])
+    sx = 2.0 * torch.arange(width, dtype=f64, device=dev) / width - 1.0
+    sy = 2.0 * torch.arange(height, dtype=f64, device=dev) / height - 1.0
+    d = (-look)[None, None, :] + (aspect * tan) * sx[None, :, None] * right - tan * sy[:, None, None] * up
+    rd = (d / torch.linalg.norm(d, dim=-1, keepdim=True)).reshape(-1, 3)
+    eye = torch.tensor(list(u.camera.camera_position[:3]), dtype=f64, device=dev)
+    out = torch.zeros((rd.shape[0], 4), dtype=torch.float32, device=dev)
+    down = rd[:, 1] < -1e-6
+    r = rd[down]
+    t0 = torch.clamp((eye[1] - amplitude) / -r[:, 1], min=0.0)
+    t1 = (eye[1] + amplitude) / -r[:, 1]
+
+    def height_at(x, z):
+        return amplitude * (0.6 * torch.sin(x / 310.0) * torch.cos(z / 260.0) + 0.4 * torch.sin((x + 2.0 * z) / 95.0))
+
+    def g(t):
+        p = eye[None, :] + t[:, None] * r
+        return p[:, 1] - height_at(p[:, 0], p[:, 2])
+
+    lo, hi = t0.clone(), t1.clone()
+    found = torch.zeros(len(r), dtype=torch.bool, device=dev)
+    prev_t, prev_g = t0, g(t0)
+    for k in range(1, coarse_steps + 1):
+        t = t0 + (t1 - t0) * (k / coarse_steps)
+        gt = g(t)
+        hit = (~found) & (prev_g > 0) & (gt <= 0)
+        lo = torch.where(hit, prev_t, lo)
+        hi = torch.where(hit, t, hi)
+        found |= hit
+        prev_t, prev_g = t, gt
+    found &= g(t0) > 0
+    for _ in range(refine_steps):
+        mid = 0.5 * (lo + hi)
+        above = g(mid) > 0
+        lo = torch.where(above, mid, lo)
+        hi = torch.where(above, hi, mid)
+    p = eye[None, :] + hi[:, None] * r
+    sel = torch.nonzero(down).squeeze(1)[found]
+    out[sel, :3] = p[found].float()
+    out[sel, 3] = 1.0
+    return out.reshape(height, width, 4)

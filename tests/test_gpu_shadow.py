@@ -109,3 +109,12 @@ def test_shadow_argument_errors(cuda, env):
     assert lib.mm_mesh_shadow(r.ctx, C.byref(u), C.byref(st2), C.byref(gb), C.c_void_p(out.data_ptr()), 256, None, 0,
                               C.byref(o), None) == L.MM_ERR_INVALID_ARGUMENT
     assert b"low_res" in lib.mm_last_error_string()
+
+
+def test_device_gbuffer_matches_host_gbuffer(cuda, mmlib):
+    import marshmallow as mm
+    u = mm.scene.uniforms(160, 90, eye=EYE, pitch=-20.0)
+    a = mm.scene.terrain_gbuffer(u, 160, 90)
+    b = mm.scene.terrain_gbuffer_cuda(u, 160, 90).cpu().numpy()
+    assert np.array_equal(a[..., 3], b[..., 3])
+    assert np.max(np.abs(a - b)) < 1e-2

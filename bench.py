@@ -49,6 +49,8 @@ def parse_args():
     ap.add_argument("--schedule", choices=["persistent", "tiled"], default="tiled")
     ap.add_argument("--density", choices=["unorm8", "fp16"], default="unorm8")
     ap.add_argument("--no-passes", action="store_true", help="skip the timings of the other passes")
+    ap.add_argument("--passes-only", action="store_true",
+                    help="time only the other passes (one march frame as their input) and print their JSON")
     return ap.parse_args()
 
 
@@ -343,6 +345,19 @@ def run_ours(args):
     for k in range(args.warmup):
         march(k)
     torch.cuda.synchronize()
+
+    if args.passes_only:
+        if rank == 0:
+            peaks_file = os.path.join(REPO, "MEASURED_PEAKS.json")
+            hbm = json.load(open(peaks_file)).get("hbm_gbs") if os.path.exists(peaks_file) else None
+            passes = measure_passes(renderer, textures, rgba, depth, uniforms, w, h, flush, stream, hbm,
+                                    world == 1 and not args.no_cpu_baseline)
+            print(json.dumps({"passes": passes, "width": w, "height": h}), flush=True)
+        renderer.close()
+        textures.close()
+        if dist:
+            dist.destroy_process_group()
+        return
 
     props = torch.cuda.get_device_properties(local)
     uuid = str(getattr(props, "uuid", "") or "")

@@ -22,13 +22,14 @@
 
 // Build knobs (defaults measured best on GB300 at 3840x2160): warps per block of the tiled kernel
 // (4 or 8) and the minimum resident blocks per SM requested from the register allocator for it
-// (4 warps x 9 blocks: 56 registers, 36 warps per SM); the same for the persistent kernel; and
-// the speculative curl fetch of the tiled march (off: it costs more occupancy than it hides).
+// (4 warps x 10 blocks: 48 registers, no spills, 40 warps per SM; 9 blocks / 56 registers was 4.6%
+// slower, 11 blocks spills); the same for the persistent kernel; and the speculative curl fetch of
+// the tiled march (off: it costs more occupancy than it hides).
 #ifndef MM_TILED_WARPS
 #define MM_TILED_WARPS 4
 #endif
 #ifndef MM_MARCH_MIN_BLOCKS
-#define MM_MARCH_MIN_BLOCKS (MM_TILED_WARPS == 4 ? 9 : 4)
+#define MM_MARCH_MIN_BLOCKS (MM_TILED_WARPS == 4 ? 10 : 5)
 #endif
 #ifndef MM_PERSISTENT_MIN_BLOCKS
 #define MM_PERSISTENT_MIN_BLOCKS 3
@@ -638,7 +639,8 @@ __device__ __forceinline__ void flush_work(unsigned long long* cnt, const Work& 
 // ------------------------------------------------------------------------------ tiled kernel
 
 // The whole of main() (:288-500) for pixel (px, py) in one thread, the shader's own loop structure.
-template <bool E, int S>
+// G = cone taps whose fetches are issued together (the densities are still added in tap order).
+template <bool E, int S, int G = MM_CONE_GROUP>
 __device__ __forceinline__ void march_pixel(const MarchLaunch& p, const Frame& f, const V3* cone, int px, int py,
                                             Work& w) {
     const Ray r = ray_setup<E, S>(p, f, px, py);
@@ -683,9 +685,9 @@ __device__ __forceinline__ void march_pixel(const MarchLaunch& p, const Frame& f
             if (density < 0.0001f) continue;
             float densityAlongLight = 0.0f;
 #pragma unroll 1
-            for (int i = 0; i < 6; i += MM_CONE_GROUP)
-                densityAlongLight = cone_taps<E, S, MM_CONE_GROUP>(p, f, cone, i, pos, stepSize, densityAlongLight,
-                                                                   w.test, w.hires);
+            for (int i = 0; i < 6; i += G)
+                densityAlongLight = cone_taps<E, S, G>(p, f, cone, i, pos, stepSize, densityAlongLight, w.test,
+                                                       w.hires);
             transmittance = shade<E>(transmittance, accum, densityAlongLight, loDensity, g.rh, r.cosTheta, r.hg);
             ++w.acc;
             if (firstT == CUDART_INF_F) firstT = t;
@@ -711,8 +713,24 @@ __device__ __forceinline__ void march_pixel(const MarchLaunch& p, const Frame& f
 // 16x8 (4 warps) pixels.
 constexpr int kBlockTileW = MM_TILED_WARPS == 8 ? 32 : 16;
 constexpr int kBlockTileH = 8;
-template <bool E, int S, bool C>
-__global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_MARCH_MIN_BLOCKS) march_tiled_kernel(MarchLaunch p) {
+
+// Full frames: one cone tap at a time (G = 1) keeps registers low enough for 10 blocks per SM, and
+// the texture unit is kept busy by the many warps.  A 1/16-pixel launch (a few waves of rays) is
+// bounded below by the latency of its longest rays (~1000 dependent fetch rounds, ~0.6 ms on
+// GB300 whatever the launch size): there the sun-cone taps are issued in pairs
+// (G = MM_PHASE16_CONE_GROUP), which shortens a sample's chain of dependent fetch rounds, with fewer
+// resident blocks (MM_PHASE16_MIN_BLOCKS) for the extra registers.  Measured at 3840x2160/16 over
+// the sweep: G = 2 / 7 blocks 0.52-0.66 ms against 0.58-0.67 ms for G = 1; G = 3 and 6 were faster
+// on some frames and slower on others.
+#ifndef MM_PHASE16_CONE_GROUP
+#define MM_PHASE16_CONE_GROUP 2
+#endif
+#ifndef MM_PHASE16_MIN_BLOCKS
+#define MM_PHASE16_MIN_BLOCKS 7
+#endif
+
+template <bool E, int S, bool C, int G>
+__device__ __forceinline__ void march_tiled_body(const MarchLaunch& p) {
     __shared__ V3 s_cone[6];
     cone_offsets(p.u, s_cone);
     __syncthreads();
@@ -731,8 +749,18 @@ __global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_MARCH_MIN_BLOCKS) marc
     if (px >= p.width || py >= p.height) return;  // :301 with the runtime image size
     const Frame f = make_frame<E>(p);
     Work w;  // work counts; dead code unless C (counters requested)
-    march_pixel<E, S>(p, f, s_cone, px, py, w);
+    march_pixel<E, S, G>(p, f, s_cone, px, py, w);
     if (C) flush_work(p.counters, w);
+}
+
+template <bool E, int S, bool C>
+__global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_MARCH_MIN_BLOCKS) march_tiled_kernel(MarchLaunch p) {
+    march_tiled_body<E, S, C, MM_CONE_GROUP>(p);
+}
+
+template <bool E, int S, bool C>
+__global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_PHASE16_MIN_BLOCKS) march_tiled_phase16_kernel(MarchLaunch p) {
+    march_tiled_body<E, S, C, MM_PHASE16_CONE_GROUP>(p);
 }
 
 // Launch order of the block rows.  A ray's cost grows as it nears the horizon (it crosses more of
@@ -771,10 +799,16 @@ int launch_tiled(const MarchLaunch& p0, cudaStream_t s) {
     }
     dim3 grid((gw + kBlockTileW - 1) / kBlockTileW, (gh + kBlockTileH - 1) / kBlockTileH);
     p.row_split = horizon_row_split(p, (int)grid.y);
-    if (p.counters)
+    if (p.pixel_mode == MM_PIXELS_PHASE16) {
+        if (p.counters)
+            march_tiled_phase16_kernel<E, S, true><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
+        else
+            march_tiled_phase16_kernel<E, S, false><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
+    } else if (p.counters) {
         march_tiled_kernel<E, S, true><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
-    else
+    } else {
         march_tiled_kernel<E, S, false><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "march_tiled_kernel launch");
     count_launch();

@@ -224,6 +224,7 @@ def measure_passes(renderer, textures, rgba, depth, uniforms, w, h, flush, strea
     import numpy as np
     import torch
     import marshmallow as mm
+    import marshmallow.lib as L
     out = {}
     src = (rgba, depth)
     dst = (torch.empty_like(rgba), torch.empty_like(depth))
@@ -246,6 +247,9 @@ def measure_passes(renderer, textures, rgba, depth, uniforms, w, h, flush, strea
     out["reproject_sweep_step"] = _pass_line(
         _median_ms(lambda: renderer.reproject(u_sweep, src, dst), flush, stream), w, h, 40.0, hbm_peak,
         "reproject.comp, every pixel, motion of one sweep step (6 deg yaw); RGBA32F + depth in and out", cpu)
+    out["reproject_sweep_step_exact"] = _pass_line(
+        _median_ms(lambda: renderer.reproject(u_sweep, src, dst, math=L.MATH_EXACT), flush, stream), w, h, 40.0,
+        hbm_peak, "the same in exact arithmetic (bit-identical to the CPU restatement)")
     out["reproject_pan_0p5deg"] = _pass_line(
         _median_ms(lambda: renderer.reproject(u_pan, src, dst), flush, stream), w, h, 40.0, hbm_peak,
         "reproject.comp, every pixel, a 0.5 deg pan")
@@ -290,7 +294,12 @@ def measure_passes(renderer, textures, rgba, depth, uniforms, w, h, flush, strea
                "sample": "oracle post chain of one %dx%d frame (%.2f s)" % (sw, sh, dt)}
     out["post_chain"] = _pass_line(
         _median_ms(lambda: renderer.post_chain(u_p, rgba, out8), flush, stream), w, h, 20.0, hbm_peak,
-        "god rays + radial blur + tonemap (two kernels); RGBA32F in, B8G8R8A8 out", cpu)
+        "god rays + radial blur + tonemap (alpha plane, god-ray plane, fused blur/tonemap; texture-unit "
+        "taps); RGBA32F in, B8G8R8A8 out", cpu)
+    out["post_chain_exact"] = _pass_line(
+        _median_ms(lambda: renderer.post_chain(u_p, rgba, out8, math=L.MATH_EXACT), flush, stream), w, h, 20.0,
+        hbm_peak, "the same in exact arithmetic with float-weight bilinear taps (bit-identical to the CPU "
+                  "restatement)")
     return out
 
 

@@ -313,12 +313,15 @@ int mm_clouds_march(mm_context ctx, const mm_uniforms* u, const mm_scene_texture
 /* The reprojection pass (reproject.comp:91-152): every pixel of dst takes the previous frame src at
  * the point where its ray meets the inner atmosphere sphere, seen by u->camera_prev (ten taps along
  * the motion vector averaged; alpha, and depth when both images have one, from the centre tap).
- * src and dst are different images of the same size.  uv = pixel / image size. */
-int mm_clouds_reproject(mm_context ctx, const mm_uniforms* u, const mm_image* src, const mm_image* dst, void* stream);
+ * src and dst are different images of the same size.  uv = pixel / image size.  opt->math (NULL =
+ * defaults, FAST): EXACT is bit-identical to the shader's arithmetic restated on the CPU; FAST
+ * uses equal algebraic forms (a tap within rounding of a pixel boundary may take the neighbour). */
+int mm_clouds_reproject(mm_context ctx, const mm_uniforms* u, const mm_image* src, const mm_image* dst,
+                        const mm_march_options* opt, void* stream);
 
 /* One frame of the reference's compute work (VulkanApplication.cpp:1053-1071): reproject prev into
  * out, then march the pixels of phase int(u->sun.color.a) (one in 16) into out.  opt->pixel_mode is
- * ignored (PHASE16). */
+ * ignored (PHASE16); opt->math applies to both passes. */
 int mm_clouds_frame(mm_context ctx, const mm_uniforms* u, const mm_scene_textures* tex, const mm_image* prev,
                     const mm_image* out, const mm_march_options* opt, void* stream);
 

@@ -340,7 +340,7 @@ int mm_context_destroy(mm_context c) {
     cudaFree(c->sur_meta);
     cudaFree(c->sur_y);
     cudaFree(c->sur_ray);
-    cudaFree(c->post_plane);
+    mm::post_state_destroy(c);
     delete c;
     return MM_OK;
 }

@@ -53,8 +53,13 @@ struct mm_context_s {
     void* sur_ray = nullptr;
     size_t sur_cap = 0, sur_pixels = 0;
     void* batch = nullptr;  // multi-view launch state (batch.cu)
-    float* post_plane = nullptr;  // god-ray term of the post chain (post.cu)
-    size_t post_plane_bytes = 0;
+    // post chain (post.cu): god-ray term and cloud alpha planes of the last frame size, with
+    // LINEAR / CLAMP texture objects on them for the production-arithmetic chain
+    float* post_plane = nullptr;
+    float* post_aplane = nullptr;
+    size_t post_pitch = 0;
+    int post_w = 0, post_h = 0;
+    cudaTextureObject_t post_gtex = 0, post_atex = 0;
 };
 
 namespace mm {
@@ -111,6 +116,7 @@ int validate_march(mm_context ctx, const mm_uniforms* u, const mm_scene_textures
 void fill_march_launch(const mm_uniforms& u, const mm_scene_textures* tex, const mm_image& out,
                        const mm_march_options& o, MarchLaunch* p);
 void batch_state_destroy(mm_context ctx);
+void post_state_destroy(mm_context ctx);
 
 #endif  // CUDA runtime available
 

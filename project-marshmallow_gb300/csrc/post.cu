@@ -75,6 +75,48 @@ int run(const PostLaunch& p, int which, int math, cudaStream_t s) {
     return post::launch<false>(p, which, s);
 }
 
+cudaTextureObject_t plane_texture(float* base, size_t pitch, int w, int h) {
+    cudaResourceDesc rd;
+    memset(&rd, 0, sizeof(rd));
+    rd.resType = cudaResourceTypePitch2D;
+    rd.res.pitch2D.devPtr = base;
+    rd.res.pitch2D.desc = cudaCreateChannelDesc<float>();
+    rd.res.pitch2D.width = (size_t)w;
+    rd.res.pitch2D.height = (size_t)h;
+    rd.res.pitch2D.pitchInBytes = pitch;
+    cudaTextureDesc td;
+    memset(&td, 0, sizeof(td));
+    td.addressMode[0] = td.addressMode[1] = cudaAddressModeClamp;  // CLAMP_TO_EDGE
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 1;
+    cudaTextureObject_t t = 0;
+    if (cudaCreateTextureObject(&t, &rd, &td, nullptr) != cudaSuccess) return 0;
+    return t;
+}
+
+// The two float planes of the chain (god-ray term, cloud alpha) for a w x h frame, with texture
+// objects; kept in the context while the frame size stays the same.
+int ensure_planes(mm_context ctx, int w, int h) {
+    if (ctx->post_plane && ctx->post_w == w && ctx->post_h == h) return MM_OK;
+    post_state_destroy(ctx);  // synchronizes with work that may still read the old planes
+    const size_t pitch = ((size_t)w * 4 + 127) / 128 * 128;
+    float* base = nullptr;
+    MM_CUDA_TRY(cudaMalloc(&base, 2 * pitch * (size_t)h));
+    ctx->post_plane = base;
+    ctx->post_aplane = reinterpret_cast<float*>(reinterpret_cast<char*>(base) + pitch * (size_t)h);
+    ctx->post_pitch = pitch;
+    ctx->post_w = w;
+    ctx->post_h = h;
+    ctx->post_gtex = plane_texture(ctx->post_plane, pitch, w, h);
+    ctx->post_atex = plane_texture(ctx->post_aplane, pitch, w, h);
+    if (!ctx->post_gtex || !ctx->post_atex) {
+        post_state_destroy(ctx);
+        return fail(MM_ERR_CUDA, "post: cannot create the plane texture objects");
+    }
+    return MM_OK;
+}
+
 bool overlaps(const mm_image* a, const mm_image* b) {
     const char* a0 = (const char*)a->rgba;
     const char* a1 = a0 + a->rgba_pitch_bytes * (size_t)a->height;
@@ -84,6 +126,17 @@ bool overlaps(const mm_image* a, const mm_image* b) {
 }
 
 }  // namespace
+
+void post_state_destroy(mm_context ctx) {
+    if (ctx->post_gtex) cudaDestroyTextureObject(ctx->post_gtex);
+    if (ctx->post_atex) cudaDestroyTextureObject(ctx->post_atex);
+    cudaFree(ctx->post_plane);
+    ctx->post_plane = ctx->post_aplane = nullptr;
+    ctx->post_gtex = ctx->post_atex = 0;
+    ctx->post_pitch = 0;
+    ctx->post_w = ctx->post_h = 0;
+}
+
 }  // namespace mm
 
 extern "C" int mm_post_options_default(mm_post_options* o) {
@@ -161,21 +214,16 @@ extern "C" int mm_post_chain(mm_context ctx, const mm_uniforms* u, const mm_imag
         if (mesh->width != clouds->width || mesh->height != clouds->height)
             return fail(MM_ERR_INVALID_ARGUMENT, "post: mesh layer and cloud image differ in size");
     }
-    const size_t plane_pitch = ((size_t)clouds->width * 4 + 127) / 128 * 128;
-    const size_t need = plane_pitch * (size_t)clouds->height;
-    if (ctx->post_plane_bytes < need) {
-        cudaFree(ctx->post_plane);  // synchronizes with work that may still read the old plane
-        ctx->post_plane = nullptr;
-        ctx->post_plane_bytes = 0;
-        MM_CUDA_TRY(cudaMalloc(&ctx->post_plane, need));
-        ctx->post_plane_bytes = need;
-    }
+    if ((r = ensure_planes(ctx, clouds->width, clouds->height))) return r;
     PostLaunch p;
     memset(&p, 0, sizeof(p));
     p.src = clouds->rgba;
     p.src_pitch = clouds->rgba_pitch_bytes;
     p.plane = ctx->post_plane;
-    p.plane_pitch = plane_pitch;
+    p.aplane = ctx->post_aplane;
+    p.plane_pitch = ctx->post_pitch;
+    p.gtex = ctx->post_gtex;
+    p.atex = ctx->post_atex;
     p.mesh = mesh ? reinterpret_cast<const float4*>(mesh->rgba) : nullptr;
     p.mesh_pitch = mesh ? mesh->rgba_pitch_bytes : 0;
     p.out8 = static_cast<uint8_t*>(out);
@@ -184,5 +232,6 @@ extern "C" int mm_post_chain(mm_context ctx, const mm_uniforms* u, const mm_imag
     p.height = clouds->height;
     p.bgra = o.bgra;
     fill_constants(u, &p);
-    return run(p, 3, o.math, (cudaStream_t)stream);
+    if (o.math == MM_MATH_EXACT) return launch_post_exact(p, 3, (cudaStream_t)stream);
+    return post::launch<false>(p, 4, (cudaStream_t)stream);
 }

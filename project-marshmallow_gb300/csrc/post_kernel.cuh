@@ -7,8 +7,10 @@
 // is two kernels: the god-ray term (the only value of the god-ray framebuffer that is not a copy
 // of the cloud image) goes to a float plane; one fused kernel then reads its ten radial-blur taps
 // from that plane, the centre colour from the cloud image, overlays the mesh, tonemaps and stores
-// 8 bits.  The three single-pass kernels (float4 in, float4 or 8 bits out) exist for callers that
-// keep the reference's intermediate framebuffers.
+// 8 bits.  In production arithmetic the chain first copies the cloud alpha into a float plane so
+// that both tap loops run on the texture unit (one filtered fetch per tap instead of four loads and
+// three lerps; 8-bit fixed-point filter weights).  The three single-pass kernels (float4 in,
+// float4 or 8 bits out) exist for callers that keep the reference's intermediate framebuffers.
 //
 // Sampling (shared with the CPU restatement): pixel (x, y) has fragUV = ((x + 0.5) / W,
 // (y + 0.5) / H); a fetch at the fragment's own uv is the texel itself (a texel centre); taps
@@ -40,6 +42,8 @@ struct PostLaunch {
     size_t mesh_pitch;
     uint8_t* out8;       // 8-bit output (tonemap, chain)
     size_t out8_pitch;
+    float* aplane;       // fast chain: the cloud image's alpha, float rows (pitch = plane_pitch)
+    cudaTextureObject_t atex, gtex;  // fast chain: LINEAR / CLAMP texture objects on aplane and plane
     int width, height;
     int night;         // sun.direction.y < 0: both passes copy the colour, alpha 1
     float sun_x, sun_y;  // sun position in NDC
@@ -76,6 +80,17 @@ __device__ __forceinline__ float bilinear(const Plane& pl, float u, float v) {
     return mixf(a, b, ay);
 }
 
+// Tap samplers: float-weight bilinear from memory (both arithmetic modes of the single passes, the
+// exact chain) or the texture unit's LINEAR filter (the fast chain; 8-bit fixed-point weights).
+struct SoftTaps {
+    Plane pl;
+    __device__ __forceinline__ float operator()(float u, float v) const { return bilinear(pl, u, v); }
+};
+struct TexTaps {
+    cudaTextureObject_t t;
+    __device__ __forceinline__ float operator()(float u, float v) const { return tex2D<float>(t, u, v); }
+};
+
 __device__ __forceinline__ void frag(int x, int y, int w, int h, float* px, float* py, float* u, float* v) {
     *u = ((float)x + 0.5f) / (float)w;
     *v = ((float)y + 0.5f) / (float)h;
@@ -84,7 +99,8 @@ __device__ __forceinline__ void frag(int x, int y, int w, int h, float* px, floa
 }
 
 // god-ray.frag:56-75 for the fragment at NDC (px, py) with centre alpha ca.
-__device__ __forceinline__ float god_ray_term(const PostLaunch& p, const Plane& alpha, float px, float py, float ca) {
+template <class Taps>
+__device__ __forceinline__ float god_ray_term(const PostLaunch& p, const Taps& alpha, float px, float py, float ca) {
     const float weight_density = 1.0f / 8.0f * 0.75f;  // SAMPLE_WEIGHT * DENSITY
     const float dx = (px - p.sun_x) * weight_density, dy = (py - p.sun_y) * weight_density;
     float accum = ca * 0.5f;
@@ -93,7 +109,7 @@ __device__ __forceinline__ float god_ray_term(const PostLaunch& p, const Plane& 
     for (int i = 0; i < 8; ++i) {
         px = px - dx;
         py = py - dy;
-        float amt = bilinear(alpha, px * 0.5f + 0.5f, py * 0.5f + 0.5f) * 0.5f;
+        float amt = alpha(px * 0.5f + 0.5f, py * 0.5f + 0.5f) * 0.5f;
         amt = amt * (1.0f / 8.0f * decay);
         accum = accum + amt;
         decay = decay * 0.99f;
@@ -102,7 +118,8 @@ __device__ __forceinline__ float god_ray_term(const PostLaunch& p, const Plane& 
 }
 
 // radialBlur.frag:127-136: the mean of ten taps of the god-ray term along the line to the sun.
-__device__ __forceinline__ float radial_term(const PostLaunch& p, const Plane& g, float px, float py) {
+template <class Taps>
+__device__ __forceinline__ float radial_term(const PostLaunch& p, const Taps& g, float px, float py) {
     float lx = p.sun_x - px, ly = p.sun_y - py;
     const float dist = sqrtf(lx * lx + ly * ly);
     lx = lx / dist;
@@ -112,7 +129,7 @@ __device__ __forceinline__ float radial_term(const PostLaunch& p, const Plane& g
 #pragma unroll
     for (int i = 0; i < 10; ++i) {
         const float ox = taps[i] * lx * 1.5f * dist, oy = taps[i] * ly * 1.5f * dist;
-        accum = accum + bilinear(g, (px + ox) * 0.5f + 0.5f, (py + oy) * 0.5f + 0.5f) * 1.1f;
+        accum = accum + g((px + ox) * 0.5f + 0.5f, (py + oy) * 0.5f + 0.5f) * 1.1f;
     }
     return accum / 10.0f;
 }
@@ -157,7 +174,7 @@ __global__ void __launch_bounds__(256) god_rays_kernel(PostLaunch p) {
     if (!p.night) {
         float px, py, u, v;
         frag(x, y, p.width, p.height, &px, &py, &u, &v);
-        const Plane alpha{p.src, p.src_pitch, 4, 3, p.width, p.height};
+        const SoftTaps alpha{Plane{p.src, p.src_pitch, 4, 3, p.width, p.height}};
         term = god_ray_term(p, alpha, px, py, c.w);
     }
     if (p.plane) {
@@ -178,7 +195,7 @@ __global__ void __launch_bounds__(256) radial_blur_kernel(PostLaunch p) {
     if (!p.night) {
         float px, py, u, v;
         frag(x, y, p.width, p.height, &px, &py, &u, &v);
-        const Plane alpha{p.src, p.src_pitch, 4, 3, p.width, p.height};
+        const SoftTaps alpha{Plane{p.src, p.src_pitch, 4, 3, p.width, p.height}};
         const float a = radial_term(p, alpha, px, py);
         o.x = p.kr * a + 0.5f * c.x;
         o.y = p.kg * a + 0.5f * c.y;
@@ -199,8 +216,9 @@ __global__ void __launch_bounds__(256) tonemap_kernel(PostLaunch p) {
 }
 
 // Radial blur of the god-ray plane + mesh overlay + tonemap, fused: src = the cloud image (whose
-// colour the god-ray framebuffer copies), plane = the god-ray term.
-template <bool E>
+// colour the god-ray framebuffer copies), plane = the god-ray term (read through the texture unit
+// when kTex).
+template <bool E, bool kTex = false>
 __global__ void __launch_bounds__(256) chain_kernel(PostLaunch p) {
     const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
     if (x >= p.width || y >= p.height) return;
@@ -220,8 +238,13 @@ __global__ void __launch_bounds__(256) chain_kernel(PostLaunch p) {
             g = c.y;
             b = c.z;
         } else {
-            const Plane term{p.plane, p.plane_pitch, 1, 0, p.width, p.height};
-            const float a = radial_term(p, term, px, py);
+            float a;
+            if (kTex) {
+                a = radial_term(p, TexTaps{p.gtex}, px, py);
+            } else {
+                const SoftTaps term{Plane{p.plane, p.plane_pitch, 1, 0, p.width, p.height}};
+                a = radial_term(p, term, px, py);
+            }
             r = p.kr * a + 0.5f * c.x;
             g = p.kg * a + 0.5f * c.y;
             b = p.kb * a + 0.5f * c.z;
@@ -230,7 +253,29 @@ __global__ void __launch_bounds__(256) chain_kernel(PostLaunch p) {
     *(reinterpret_cast<uint32_t*>(p.out8 + (size_t)y * p.out8_pitch) + x) = tonemap8<E>(p, r, g, b, u, v);
 }
 
-// which: 0 god rays, 1 radial blur, 2 tonemap, 3 chain (god-ray plane, then the fused kernel).
+// Fast chain, first kernel: the cloud image's alpha into a float plane (read by the texture unit).
+template <bool E>
+__global__ void __launch_bounds__(256) alpha_plane_kernel(PostLaunch p) {
+    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+    if (x >= p.width || y >= p.height) return;
+    *(reinterpret_cast<float*>(reinterpret_cast<char*>(p.aplane) + (size_t)y * p.plane_pitch) + x) =
+        ld4(p.src, p.src_pitch, x, y).w;
+}
+
+// Fast chain, second kernel: the god-ray term with its eight taps filtered by the texture unit.
+template <bool E>
+__global__ void __launch_bounds__(256) god_rays_tex_kernel(PostLaunch p) {
+    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+    if (x >= p.width || y >= p.height) return;
+    float px, py, u, v;
+    frag(x, y, p.width, p.height, &px, &py, &u, &v);
+    const float ca = *(reinterpret_cast<const float*>(reinterpret_cast<const char*>(p.aplane) + (size_t)y * p.plane_pitch) + x);
+    *(reinterpret_cast<float*>(reinterpret_cast<char*>(p.plane) + (size_t)y * p.plane_pitch) + x) =
+        god_ray_term(p, TexTaps{p.atex}, px, py, ca);
+}
+
+// which: 0 god rays, 1 radial blur, 2 tonemap, 3 chain (god-ray plane, then the fused kernel),
+// 4 fast chain (alpha plane, god-ray plane with texture-unit taps, fused kernel with texture-unit taps).
 template <bool E>
 int launch(const PostLaunch& p, int which, cudaStream_t s) {
     const dim3 block(32, 8), grid((p.width + 31) / 32, (p.height + 7) / 8);
@@ -238,6 +283,17 @@ int launch(const PostLaunch& p, int which, cudaStream_t s) {
         case 0: god_rays_kernel<E><<<grid, block, 0, s>>>(p); break;
         case 1: radial_blur_kernel<E><<<grid, block, 0, s>>>(p); break;
         case 2: tonemap_kernel<E><<<grid, block, 0, s>>>(p); break;
+        case 4:
+            if (!p.night) {
+                alpha_plane_kernel<E><<<grid, block, 0, s>>>(p);
+                count_launch();
+                MM_CUDA_TRY(cudaGetLastError());
+                god_rays_tex_kernel<E><<<grid, block, 0, s>>>(p);
+                count_launch();
+                MM_CUDA_TRY(cudaGetLastError());
+            }
+            chain_kernel<E, true><<<grid, block, 0, s>>>(p);
+            break;
         default:
             if (!p.night) {
                 god_rays_kernel<E><<<grid, block, 0, s>>>(p);

@@ -1,4 +1,5 @@
-// reproject.cu - the reprojection pass of reproject.comp:91-152 (mm_clouds_reproject) and the
+// reproject.cu - the reprojection pass of reproject.comp:91-152 (mm_clouds_reproject; this file
+// holds the exact-arithmetic kernel, reproject_fast.cu the production one) and the
 // reference's per-frame compute work (mm_clouds_frame: reprojection of every pixel, then the march
 // of one pixel in 16, VulkanApplication.cpp:1053-1071).
 //
@@ -107,10 +108,16 @@ __global__ void __launch_bounds__(256) reproject_kernel(P p) {
 }  // namespace rep
 }  // namespace mm
 
+namespace mm {
+int launch_reproject_fast(const mm_uniforms& u, const mm_image& src, const mm_image& dst, cudaStream_t s);
+}
+
 extern "C" int mm_clouds_reproject(mm_context ctx, const mm_uniforms* u, const mm_image* src, const mm_image* dst,
-                                   void* stream) {
+                                   const mm_march_options* opt, void* stream) {
     using mm::fail;
     if (!ctx || !u || !src || !dst) return fail(MM_ERR_INVALID_ARGUMENT, "reproject: null argument");
+    const int math = opt ? opt->math : MM_MATH_FAST;
+    if (math != MM_MATH_FAST && math != MM_MATH_EXACT) return fail(MM_ERR_INVALID_ARGUMENT, "reproject: bad math %d", math);
     if (!src->rgba || !dst->rgba || src->width != dst->width || src->height != dst->height || dst->width <= 0 ||
         dst->height <= 0 || dst->width > 32768 || dst->height > 32768)
         return fail(MM_ERR_INVALID_ARGUMENT, "reproject: source and target must be images of the same size");
@@ -121,6 +128,7 @@ extern "C" int mm_clouds_reproject(mm_context ctx, const mm_uniforms* u, const m
     if ((src->depth && src->depth_pitch_bytes < (size_t)src->width * 4) ||
         (dst->depth && dst->depth_pitch_bytes < (size_t)dst->width * 4))
         return fail(MM_ERR_INVALID_ARGUMENT, "reproject: bad depth pitch");
+    if (math == MM_MATH_FAST) return mm::launch_reproject_fast(*u, *src, *dst, (cudaStream_t)stream);
     mm::rep::P p;
     p.u = *u;
     p.src = reinterpret_cast<const float4*>(src->rgba);
@@ -149,6 +157,6 @@ extern "C" int mm_clouds_frame(mm_context ctx, const mm_uniforms* u, const mm_sc
     o.pixel_mode = MM_PIXELS_PHASE16;
     int r = mm::validate_march(ctx, u, tex, out, &o);
     if (r) return r;
-    if ((r = mm_clouds_reproject(ctx, u, prev, out, stream))) return r;
+    if ((r = mm_clouds_reproject(ctx, u, prev, out, &o, stream))) return r;
     return mm_clouds_march(ctx, u, tex, out, &o, stream);
 }

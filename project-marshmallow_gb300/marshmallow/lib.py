@@ -122,7 +122,8 @@ SIGNATURES = {
     "mm_context_destroy": (C.c_int, [C.c_void_p]),
     "mm_clouds_march": (C.c_int, [C.c_void_p, C.POINTER(Uniforms), C.POINTER(SceneTextures), C.POINTER(Image),
                                   C.POINTER(MarchOptions), C.c_void_p]),
-    "mm_clouds_reproject": (C.c_int, [C.c_void_p, C.POINTER(Uniforms), C.POINTER(Image), C.POINTER(Image), C.c_void_p]),
+    "mm_clouds_reproject": (C.c_int, [C.c_void_p, C.POINTER(Uniforms), C.POINTER(Image), C.POINTER(Image),
+                                      C.POINTER(MarchOptions), C.c_void_p]),
     "mm_clouds_frame": (C.c_int, [C.c_void_p, C.POINTER(Uniforms), C.POINTER(SceneTextures), C.POINTER(Image),
                                   C.POINTER(Image), C.POINTER(MarchOptions), C.c_void_p]),
     "mm_mesh_shadow": (C.c_int, [C.c_void_p, C.POINTER(Uniforms), C.POINTER(SceneTextures), C.POINTER(GBuffer),

@@ -156,10 +156,10 @@ class Renderer:
         return L.Image(rgba.data_ptr(), rgba.stride(0) * 4, depth.data_ptr() if depth is not None else None,
                        depth.stride(0) * 4 if depth is not None else 0, w, h)
 
-    def reproject(self, u, src, dst, stream=None):
-        """src, dst: (rgba, depth) tensor pairs of the same size."""
+    def reproject(self, u, src, dst, stream=None, **opts):
+        """src, dst: (rgba, depth) tensor pairs of the same size; opts: math=L.MATH_EXACT / MATH_FAST."""
         L.check(self.lib.mm_clouds_reproject(self.ctx, C.byref(u), C.byref(self.image(*src)), C.byref(self.image(*dst)),
-                                             _stream_ptr(stream)), "mm_clouds_reproject")
+                                             C.byref(self.options(**opts)), _stream_ptr(stream)), "mm_clouds_reproject")
 
     def frame(self, u, textures, prev, out, stream=None, **opts):
         o = self.options(**opts)

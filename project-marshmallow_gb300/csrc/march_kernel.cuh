@@ -628,12 +628,19 @@ struct Work {
     unsigned long long test = 0, hires = 0, iter = 0, acc = 0;
 };
 
+// Adds a thread's work counts to the launch totals: summed over the warp's active lanes first (one
+// ray's counts fit 32 bits), then one atomic per counter from the lowest active lane.
 __device__ __forceinline__ void flush_work(unsigned long long* cnt, const Work& w) {
     if (!cnt) return;
-    atomicAdd(cnt + 0, w.test);
-    atomicAdd(cnt + 1, w.hires);
-    atomicAdd(cnt + 2, w.iter);
-    atomicAdd(cnt + 3, w.acc);
+    const unsigned mask = __activemask();
+    const unsigned t = __reduce_add_sync(mask, (unsigned)w.test), h = __reduce_add_sync(mask, (unsigned)w.hires);
+    const unsigned i = __reduce_add_sync(mask, (unsigned)w.iter), a = __reduce_add_sync(mask, (unsigned)w.acc);
+    if ((threadIdx.x & 31) == (unsigned)(__ffs(mask) - 1)) {
+        atomicAdd(cnt + 0, (unsigned long long)t);
+        atomicAdd(cnt + 1, (unsigned long long)h);
+        atomicAdd(cnt + 2, (unsigned long long)i);
+        atomicAdd(cnt + 3, (unsigned long long)a);
+    }
 }
 
 // ------------------------------------------------------------------------------ tiled kernel

@@ -55,6 +55,7 @@ struct mm_context_s {
     void* batch = nullptr;  // multi-view launch state (batch.cu)
     // post chain (post.cu): god-ray term and cloud alpha planes of the last frame size, with
     // LINEAR / CLAMP texture objects on them for the production-arithmetic chain
+    void* post_raw = nullptr;  // the allocation holding both planes
     float* post_plane = nullptr;
     float* post_aplane = nullptr;
     size_t post_pitch = 0;

@@ -100,11 +100,20 @@ cudaTextureObject_t plane_texture(float* base, size_t pitch, int w, int h) {
 int ensure_planes(mm_context ctx, int w, int h) {
     if (ctx->post_plane && ctx->post_w == w && ctx->post_h == h) return MM_OK;
     post_state_destroy(ctx);  // synchronizes with work that may still read the old planes
-    const size_t pitch = ((size_t)w * 4 + 127) / 128 * 128;
-    float* base = nullptr;
-    MM_CUDA_TRY(cudaMalloc(&base, 2 * pitch * (size_t)h));
-    ctx->post_plane = base;
-    ctx->post_aplane = reinterpret_cast<float*>(reinterpret_cast<char*>(base) + pitch * (size_t)h);
+    // A texture object's base address must be a multiple of the device's texture alignment and its
+    // pitch a multiple of the texture pitch alignment: both planes start on such a boundary.
+    int align = 512, pitch_align = 32;
+    cudaDeviceGetAttribute(&align, cudaDevAttrTextureAlignment, ctx->device);
+    cudaDeviceGetAttribute(&pitch_align, cudaDevAttrTexturePitchAlignment, ctx->device);
+    const size_t pa = (size_t)(pitch_align > 128 ? pitch_align : 128), ba = (size_t)(align > 256 ? align : 256);
+    const size_t pitch = ((size_t)w * 4 + pa - 1) / pa * pa;
+    const size_t plane = (pitch * (size_t)h + ba - 1) / ba * ba;
+    char* raw = nullptr;
+    MM_CUDA_TRY(cudaMalloc(&raw, 2 * plane + ba));
+    char* base = raw + ((ba - ((uintptr_t)raw % ba)) % ba);
+    ctx->post_raw = raw;
+    ctx->post_plane = reinterpret_cast<float*>(base);
+    ctx->post_aplane = reinterpret_cast<float*>(base + plane);
     ctx->post_pitch = pitch;
     ctx->post_w = w;
     ctx->post_h = h;
@@ -130,7 +139,8 @@ bool overlaps(const mm_image* a, const mm_image* b) {
 void post_state_destroy(mm_context ctx) {
     if (ctx->post_gtex) cudaDestroyTextureObject(ctx->post_gtex);
     if (ctx->post_atex) cudaDestroyTextureObject(ctx->post_atex);
-    cudaFree(ctx->post_plane);
+    cudaFree(ctx->post_raw);
+    ctx->post_raw = nullptr;
     ctx->post_plane = ctx->post_aplane = nullptr;
     ctx->post_gtex = ctx->post_atex = 0;
     ctx->post_pitch = 0;

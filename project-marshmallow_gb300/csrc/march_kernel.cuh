@@ -646,8 +646,10 @@ __device__ __forceinline__ void flush_work(unsigned long long* cnt, const Work& 
 // ------------------------------------------------------------------------------ tiled kernel
 
 // The whole of main() (:288-500) for pixel (px, py) in one thread, the shader's own loop structure.
-// G = cone taps whose fetches are issued together (the densities are still added in tap order).
-template <bool E, int S, int G = MM_CONE_GROUP>
+// G = cone taps whose fetches are issued together (the densities are still added in tap order);
+// SC = in small-step mode, issue the sample's curl fetch with its cloudTest fetches (speculative:
+// used only if the sample has density).
+template <bool E, int S, int G = MM_CONE_GROUP, bool SC = (MM_SPEC_CURL != 0)>
 __device__ __forceinline__ void march_pixel(const MarchLaunch& p, const Frame& f, const V3* cone, int px, int py,
                                             Work& w) {
     const Ray r = ray_setup<E, S>(p, f, px, py);
@@ -668,12 +670,10 @@ __device__ __forceinline__ void march_pixel(const MarchLaunch& p, const Frame& f
         ++w.iter;
         const V3 pos = f.cam + t * rd;
         const Geo g = geo_at<E>(f, pos);
-#if MM_SPEC_CURL
         // Once the ray marches in small steps, a sample that finds density goes on to cloudHiRes;
-        // its curl fetch is issued with the cloudTest fetches so the two latencies overlap.
+        // with SC its curl fetch is issued with the cloudTest fetches so the two latencies overlap.
         V3 qh;
-        if (!noHits) qh = hires_point<E, S>(p, g, stepSize);
-#endif
+        if (SC && !noHits) qh = hires_point<E, S>(p, g, stepSize);
         float density = cloud_test<E, S>(p, f, g, w.test);
         const float loDensity = density;
         if (density > 0.0f) {
@@ -684,11 +684,10 @@ __device__ __forceinline__ void march_pixel(const MarchLaunch& p, const Frame& f
                 noHits = false;
                 continue;
             }
-#if MM_SPEC_CURL
-            density = hires_finish<E>(hires_fetch<E, S>(p, qh), g.rh, density, w.hires);
-#else
-            density = cloud_hires<E, S>(p, g, stepSize, density, w.hires);
-#endif
+            if (SC)
+                density = hires_finish<E>(hires_fetch<E, S>(p, qh), g.rh, density, w.hires);
+            else
+                density = cloud_hires<E, S>(p, g, stepSize, density, w.hires);
             if (density < 0.0001f) continue;
             float densityAlongLight = 0.0f;
 #pragma unroll 1
@@ -721,22 +720,33 @@ __device__ __forceinline__ void march_pixel(const MarchLaunch& p, const Frame& f
 constexpr int kBlockTileW = MM_TILED_WARPS == 8 ? 32 : 16;
 constexpr int kBlockTileH = 8;
 
-// Full frames: one cone tap at a time (G = 1) keeps registers low enough for 10 blocks per SM, and
-// the texture unit is kept busy by the many warps.  A 1/16-pixel launch (a few waves of rays) is
-// bounded below by the latency of its longest rays (~1000 dependent fetch rounds, ~0.6 ms on
-// GB300 whatever the launch size): there the sun-cone taps are issued in pairs
-// (G = MM_PHASE16_CONE_GROUP), which shortens a sample's chain of dependent fetch rounds, with fewer
-// resident blocks (MM_PHASE16_MIN_BLOCKS) for the extra registers.  Measured at 3840x2160/16 over
-// the sweep: G = 2 / 7 blocks 0.52-0.66 ms against 0.58-0.67 ms for G = 1; G = 3 and 6 were faster
-// on some frames and slower on others.
+// Three variants of the same march, chosen per launch:
+//  - full frames: one cone tap at a time (G = 1) keeps registers low enough for 10 blocks per SM,
+//    and the texture unit is kept busy by the many warps;
+//  - launches of at most kLatencyRays rays (a 1920x1080 frame at 1/16 of its pixels, or a small
+//    image): such a launch is bounded below by the latency of its longest rays (~1000 dependent
+//    fetch rounds just above the horizon, ~0.6 ms on GB300 whatever the launch size), so all six
+//    sun-cone taps of a sample are issued together (G = 6: a sample's cone takes 3 dependent fetch
+//    rounds instead of up to 18) at 3 blocks per SM for the registers;
+//  - larger 1/16-pixel launches (3840x2160/16: several waves): cone taps in pairs (G = 2, 7 blocks).
+// Measured over the 16-frame sweep (mean of frames 0, 5, 10, 15): 1920x1080/16 0.67 ms (G = 1),
+// 0.58 (G = 2), 0.50 (G = 6); 3840x2160/16 0.65 (G = 1), 0.60 (G = 2), 0.73 (G = 6).  Issuing the
+// curl fetch speculatively with the cloudTest fetches (SC) did not help.
 #ifndef MM_PHASE16_CONE_GROUP
 #define MM_PHASE16_CONE_GROUP 2
 #endif
 #ifndef MM_PHASE16_MIN_BLOCKS
 #define MM_PHASE16_MIN_BLOCKS 7
 #endif
+#ifndef MM_PHASE16_SPEC_CURL
+#define MM_PHASE16_SPEC_CURL 0
+#endif
+#ifndef MM_LATENCY_MIN_BLOCKS
+#define MM_LATENCY_MIN_BLOCKS 3
+#endif
+constexpr long long kLatencyRays = 262144;
 
-template <bool E, int S, bool C, int G>
+template <bool E, int S, bool C, int G, bool SC>
 __device__ __forceinline__ void march_tiled_body(const MarchLaunch& p) {
     __shared__ V3 s_cone[6];
     cone_offsets(p.u, s_cone);
@@ -756,18 +766,23 @@ __device__ __forceinline__ void march_tiled_body(const MarchLaunch& p) {
     if (px >= p.width || py >= p.height) return;  // :301 with the runtime image size
     const Frame f = make_frame<E>(p);
     Work w;  // work counts; dead code unless C (counters requested)
-    march_pixel<E, S, G>(p, f, s_cone, px, py, w);
+    march_pixel<E, S, G, SC>(p, f, s_cone, px, py, w);
     if (C) flush_work(p.counters, w);
 }
 
 template <bool E, int S, bool C>
 __global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_MARCH_MIN_BLOCKS) march_tiled_kernel(MarchLaunch p) {
-    march_tiled_body<E, S, C, MM_CONE_GROUP>(p);
+    march_tiled_body<E, S, C, MM_CONE_GROUP, (MM_SPEC_CURL != 0)>(p);
 }
 
 template <bool E, int S, bool C>
 __global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_PHASE16_MIN_BLOCKS) march_tiled_phase16_kernel(MarchLaunch p) {
-    march_tiled_body<E, S, C, MM_PHASE16_CONE_GROUP>(p);
+    march_tiled_body<E, S, C, MM_PHASE16_CONE_GROUP, (MM_PHASE16_SPEC_CURL != 0)>(p);
+}
+
+template <bool E, int S, bool C>
+__global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_LATENCY_MIN_BLOCKS) march_tiled_latency_kernel(MarchLaunch p) {
+    march_tiled_body<E, S, C, 6, false>(p);
 }
 
 // Launch order of the block rows.  A ray's cost grows as it nears the horizon (it crosses more of
@@ -806,7 +821,12 @@ int launch_tiled(const MarchLaunch& p0, cudaStream_t s) {
     }
     dim3 grid((gw + kBlockTileW - 1) / kBlockTileW, (gh + kBlockTileH - 1) / kBlockTileH);
     p.row_split = horizon_row_split(p, (int)grid.y);
-    if (p.pixel_mode == MM_PIXELS_PHASE16) {
+    if ((long long)gw * gh <= kLatencyRays) {
+        if (p.counters)
+            march_tiled_latency_kernel<E, S, true><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
+        else
+            march_tiled_latency_kernel<E, S, false><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
+    } else if (p.pixel_mode == MM_PIXELS_PHASE16) {
         if (p.counters)
             march_tiled_phase16_kernel<E, S, true><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
         else

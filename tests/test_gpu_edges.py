@@ -149,3 +149,24 @@ def test_size_limits(cuda, mmlib, env):
         assert mmlib.mm_mesh_shadow(r.ctx, C.byref(u), C.byref(st), C.byref(gb), C.c_void_p(buf.data_ptr()),
                                     1 << 20, None, 0, C.byref(o), None) == L.MM_ERR_INVALID_ARGUMENT
     cuda.cuda.synchronize()
+
+
+def test_kernel_variants_exact(cuda, orc, oracle_textures, env):
+    # The march picks one of three kernels per launch (full frames, launches of <= 262144 rays,
+    # larger 1/16-pixel launches); all three are the same arithmetic and equal the oracle bit for bit.
+    import marshmallow as mm
+    import marshmallow.lib as L
+    tex, r = env
+    for (w, h, mode) in [(2880, 1620, 1), (640, 400, 0), (640, 400, 1)]:
+        u = mm.scene.uniforms(w, h, yaw=30.0, pitch=10.0, time=1.0)
+        u.sun.color[3] = 9.0
+        rgba = cuda.zeros((h, w, 4), device="cuda")
+        dep = cuda.zeros((h, w), device="cuda")
+        r.march(u, tex, rgba, dep, pixel_mode=mode, math=L.MATH_EXACT, sampler=L.SAMPLER_SOFTWARE)
+        cuda.cuda.synchronize()
+        want, wd, _ = orc.march(u, oracle_textures, w, h, pixel_mode=mode)
+        got, gd = rgba.cpu().numpy(), dep.cpu().numpy()
+        if mode:
+            got, gd, want, wd = got[2::4, 1::4], gd[2::4, 1::4], want[2::4, 1::4], wd[2::4, 1::4]
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (w, h, mode)
+        assert np.array_equal(gd.view(np.uint32), wd.view(np.uint32)), (w, h, mode)

@@ -115,6 +115,22 @@ class ClockSampler:
 # ------------------------------------------------------------------------------ shared
 
 
+def reduce_max(value, dist, device):
+    """The maximum of `value` over all ranks (the slowest rank's time); `dist` None = one process."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world, units_per_rank, seconds):
+    """Whole-job throughput of `world` replicas that each processed `units_per_rank` units, timed by
+    the slowest rank (`seconds`): replicas only, no collective on the data path."""
+    return world * units_per_rank / seconds
+
+
 def sweep(k):
     import marshmallow as mm
     return mm.scene.sweep_params(k % SWEEP, SWEEP)
@@ -388,13 +404,9 @@ def run_ours(args):
         dist.barrier()
     clocks = sampler.stop()
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms = sum(step_ms)
-    if dist:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = reduce_max(sum(step_ms), dist, "cuda")
     rays_per_frame = w * h
-    value = world * rays_per_frame * args.steps / (total_ms * 1e-3) / 1e6
+    value = whole_job_rate(world, rays_per_frame * args.steps, total_ms * 1e-3) / 1e6
     ms_frame = total_ms / args.steps
 
     # Algorithmic work of the timed frames (same frames, counted in a separate untimed pass).
@@ -457,12 +469,8 @@ def run_ours(args):
                 host_depth[b].copy_(dev_depth[b], non_blocking=True)
             done_cpy[b].record(s_cpy)
         torch.cuda.synchronize()
-        e2e_s = time.perf_counter() - t0
-        if dist:
-            t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
-        e2e = {"value": round(world * rays_per_frame * args.steps / e2e_s / 1e6, 3), "unit": "Mrays/s",
+        e2e_s = reduce_max(time.perf_counter() - t0, dist, "cuda")
+        e2e = {"value": round(whole_job_rate(world, rays_per_frame * args.steps, e2e_s) / 1e6, 3), "unit": "Mrays/s",
                "h2d_bytes_per_step": C.sizeof(L.Uniforms), "d2h_bytes_per_step": 20 * rays_per_frame,
                "ms_per_step": round(1e3 * e2e_s / args.steps, 3)}
 

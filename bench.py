@@ -47,7 +47,7 @@ def parse_args():
     ap.add_argument("--sampler", choices=["hardware", "software"], default="hardware")
     ap.add_argument("--math", choices=["fast", "exact"], default="fast")
     ap.add_argument("--schedule", choices=["persistent", "tiled"], default="tiled")
-    ap.add_argument("--density", choices=["unorm8", "fp16"], default="unorm8")
+    ap.add_argument("--density", choices=["unorm8", "fp16", "bf16"], default="unorm8")
     ap.add_argument("--no-passes", action="store_true", help="skip the timings of the other passes")
     ap.add_argument("--passes-only", action="store_true",
                     help="time only the other passes (one march frame as their input) and print their JSON")
@@ -350,7 +350,7 @@ def run_ours(args):
     sptr = C.c_void_p(stream.cuda_stream)
 
     textures = mm.render.Textures(seed=0)
-    density_format = L.FORMAT_FP16 if args.density == "fp16" else L.FORMAT_UNORM8
+    density_format = {"unorm8": L.FORMAT_UNORM8, "fp16": L.FORMAT_FP16, "bf16": L.FORMAT_BF16}[args.density]
     if density_format != L.FORMAT_UNORM8:
         textures.set_density_format(density_format)
     renderer = mm.render.Renderer()

@@ -126,7 +126,8 @@ typedef enum mm_noise_kind {
 typedef enum mm_texel_format {
     MM_FORMAT_UNORM8 = 0, /* texel/255, as VK_FORMAT_R8G8B8A8_UNORM (Texture.h:29) */
     MM_FORMAT_FP16 = 1,   /* IEEE half, value = texel/255 rounded to half */
-    MM_FORMAT_BF16 = 2    /* bfloat16, value = texel/255 rounded to bf16 */
+    MM_FORMAT_BF16 = 2    /* bfloat16, value = texel/255 rounded to bf16 (held exactly in an FP16 array: the
+                             CUDA runtime has no bfloat16 texture channel kind) */
 } mm_texel_format;
 
 typedef struct mm_noise_desc {

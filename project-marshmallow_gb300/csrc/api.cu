@@ -67,9 +67,18 @@ int resolve_desc(const mm_noise_desc* d, int* w, int* h, int* z, int* ch) {
 
 // Hardware-filtered copy: CUDA array of the texel format with a LINEAR/WRAP/normalized texture
 // object (the reference samplers, Texture.cpp:29-52 and 315-338).
-__global__ void unorm8_to_half(const uint8_t* in, __half* out, size_t n) {
+// texel/255 rounded to FP16 (bf16 == false) or to bfloat16 (bf16 == true; round to nearest even on
+// the float's bits).  A bfloat16 value of texel/255 (8 significant bits, >= 1/255 or 0) is exactly
+// an FP16 value, so both are stored in FP16 arrays and filtered by the texture unit's FP16 path.
+__global__ void unorm8_to_half(const uint8_t* in, __half* out, size_t n, bool bf16) {
     size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (i < n) out[i] = __float2half_rn(__fdiv_rn((float)in[i], 255.0f));
+    if (i >= n) return;
+    float v = __fdiv_rn((float)in[i], 255.0f);
+    if (bf16) {
+        const uint32_t b = __float_as_uint(v);
+        v = __uint_as_float((b + 0x7FFFu + ((b >> 16) & 1u)) & 0xFFFF0000u);
+    }
+    out[i] = __float2half_rn(v);
 }
 
 int build_hw_copy(mm_texture t, int format, cudaStream_t s) {
@@ -87,13 +96,11 @@ int build_hw_copy(mm_texture t, int format, cudaStream_t s) {
     if (format == MM_FORMAT_UNORM8) {
         cd = cudaCreateChannelDesc(8, ch >= 2 ? 8 : 0, ch >= 4 ? 8 : 0, ch >= 4 ? 8 : 0, cudaChannelFormatKindUnsigned);
         elem = 1;
-    } else if (format == MM_FORMAT_FP16) {
+    } else if (format == MM_FORMAT_FP16 || format == MM_FORMAT_BF16) {
+        // The CUDA runtime has no bfloat16 channel kind; bfloat16-rounded texels are held in an FP16
+        // array (exactly, see unorm8_to_half) and filtered by the FP16 path.
         cd = cudaCreateChannelDesc(16, ch >= 2 ? 16 : 0, ch >= 4 ? 16 : 0, ch >= 4 ? 16 : 0, cudaChannelFormatKindFloat);
         elem = 2;
-    } else if (format == MM_FORMAT_BF16) {
-        // The CUDA runtime has no bfloat16 channel kind, so a bf16 copy cannot be filtered by the
-        // texture unit.
-        return fail(MM_ERR_UNSUPPORTED, "texture: no hardware-filtered bf16 format");
     } else {
         return fail(MM_ERR_INVALID_ARGUMENT, "texture: unknown format %d", format);
     }
@@ -106,7 +113,7 @@ int build_hw_copy(mm_texture t, int format, cudaStream_t s) {
     if (format != MM_FORMAT_UNORM8) {
         MM_CUDA_TRY(cudaMallocAsync(&conv, n * elem, s));
         const unsigned blocks = (unsigned)((n + 255) / 256);
-        unorm8_to_half<<<blocks, 256, 0, s>>>(t->texels, (__half*)conv, n);
+        unorm8_to_half<<<blocks, 256, 0, s>>>(t->texels, (__half*)conv, n, format == MM_FORMAT_BF16);
         MM_CUDA_TRY(cudaGetLastError());
         mm::count_launch();
         src = conv;

@@ -1,7 +1,7 @@
 """Precision sweep: 3840x2160 frames over sun elevation {5, 30, 60, 85} deg x coverage offset
-{-0.2, 0, +0.2}, UNORM8 and FP16 density textures, production arithmetic, against the FP64 oracle on
-every 8th row and column.  Gates: UNORM8 RMSE <= 1/255 and p99.9 <= 4/255; FP16 RMSE <= 2/255
-(the mixed-precision gate) with at most 0.5% of pixels above 4/255.  FP16 is less accurate than
+{-0.2, 0, +0.2}, UNORM8, FP16 and BF16 density textures, production arithmetic, against the FP64
+oracle on every 8th row and column.  Gates: UNORM8 RMSE <= 1/255 and p99.9 <= 4/255; FP16 and BF16
+RMSE <= 2/255 (the mixed-precision gate) with at most 0.5% (FP16) / 5% (BF16) of pixels above 4/255.  FP16 is less accurate than
 UNORM8 here: the texels themselves are k/255 rounded to 11 bits, and the texture unit filters them at
 reduced precision.  Prints the table of errors (colour in 1/255 of the reference tonemap, depth
 relative)."""
@@ -25,12 +25,12 @@ def setup(cuda, mmlib):
     t.close()
 
 
-@pytest.mark.parametrize("fmt", ["unorm8", "fp16"])
+@pytest.mark.parametrize("fmt", ["unorm8", "fp16", "bf16"])
 def test_precision_sweep_4k(cuda, orc, setup, fmt):
     import marshmallow as mm
     import marshmallow.lib as L
     tex, r, host = setup
-    f = L.FORMAT_FP16 if fmt == "fp16" else L.FORMAT_UNORM8
+    f = {"unorm8": L.FORMAT_UNORM8, "fp16": L.FORMAT_FP16, "bf16": L.FORMAT_BF16}[fmt]
     tex.set_density_format(f)
     rows = []
     try:
@@ -54,6 +54,11 @@ def test_precision_sweep_4k(cuda, orc, setup, fmt):
         if fmt == "fp16":
             assert e["rmse_255"] <= 2.0, (el, off, e)
             assert e["frac_over_4"] <= 0.005, (el, off, e)
+        elif fmt == "bf16":
+            # bfloat16 keeps 8 significant bits: texel/255 moves by up to half a bf16 step, which
+            # flips more density thresholds (measured: RMSE 0.73-1.87/255, 1-3.4% of pixels > 4/255)
+            assert e["rmse_255"] <= 2.0, (el, off, e)
+            assert e["frac_over_4"] <= 0.05, (el, off, e)
         else:
             assert e["rmse_255"] <= 1.0, (el, off, e)
             assert e["p999_255"] <= 4.0, (el, off, e)

@@ -49,6 +49,9 @@ def parse_args():
     ap.add_argument("--schedule", choices=["persistent", "tiled"], default="tiled")
     ap.add_argument("--density", choices=["unorm8", "fp16", "bf16"], default="unorm8")
     ap.add_argument("--no-passes", action="store_true", help="skip the timings of the other passes")
+    ap.add_argument("--batch", action="store_true",
+                    help="time the uneven-view batch (mm_clouds_march_batch) instead of the 4K frame")
+    ap.add_argument("--batch-views", type=int, default=70, help="first N views of the 70-view batch")
     ap.add_argument("--passes-only", action="store_true",
                     help="time only the other passes (one march frame as their input) and print their JSON")
     return ap.parse_args()
@@ -531,10 +534,73 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_batch(args):
+    """Many views in one launch: the seeded 70-view batch (6 cube-map faces at 512^2, 32 cameras at
+    640x360-1920x1080, 32 cameras at 3840x2160 with random sun and yaw), one mm_clouds_march_batch
+    per step with the schedule and tile shape the autotuner picks; beside it the same views as one
+    launch each."""
+    import torch
+    import marshmallow as mm
+    rank, world, local = rank_info()
+    torch.cuda.set_device(local)
+    if rank != 0:
+        return
+    tex = mm.render.Textures(seed=0)
+    r = mm.render.Renderer()
+    views = mm.scene.batch_views(seed=0)[:max(1, args.batch_views)]
+    outs = [(torch.empty((h, w, 4), device="cuda"), torch.empty((h, w), device="cuda")) for w, h, _ in views]
+    rays = sum(w * h for w, h, _ in views)
+    arr = r.march_batch(views, tex, outs)
+    best, table = r.autotune_batch(arr, len(views), tex)
+    opts = dict(warp_tile_w=best.warp_tile_w, tiles_per_grab=best.tiles_per_grab, schedule=best.schedule)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, k):
+        ts = []
+        for i in range(args.warmup + k):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            if i >= args.warmup:
+                ts.append(a.elapsed_time(b))
+        return ts
+
+    lib = mm.lib.load()
+    l0 = lib.mm_kernel_launch_count()
+    ts = timed(lambda: r.march_batch(views, tex, outs, **opts), args.steps)
+    launches = lib.mm_kernel_launch_count() - l0
+    seq = timed(lambda: [r.march(u, tex, o[0], o[1]) for (w, h, u), o in zip(views, outs)], max(1, args.steps // 4))
+    ms = sum(ts) / len(ts)
+    ms_seq = sum(seq) / len(seq)
+    line = {
+        "metric": "Mrays/s, %d views of uneven resolution in one batched launch" % len(views),
+        "value": round(rays / ms / 1e3, 2),
+        "unit": "Mrays/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "seeded uneven-view batch (cube faces 512^2, 640x360-1920x1080 cameras, 3840x2160 "
+                               "cameras with random sun 5-85 deg and yaw 0-360 deg)", "views": len(views),
+                   "mrays_per_step": round(rays / 1e6, 2),
+                   "schedule": {0: "persistent", 1: "blocks", 2: "graph"}[best.schedule],
+                   "warp_tile_w": best.warp_tile_w, "tiles_per_grab": best.tiles_per_grab,
+                   "l2": "flushed between steps"},
+        "one_launch_per_view_ms": round(ms_seq, 3), "autotune_ms": [round(v, 2) for v in table],
+        "gpu_launches": int(launches),
+    }
+    print(json.dumps(line), flush=True)
+    r.close()
+    tex.close()
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.batch:
+        run_batch(args)
     else:
         run_ours(args)
 

@@ -401,25 +401,37 @@ typedef struct mm_view {
     float coverage_offset;
 } mm_view;
 
+typedef enum mm_batch_schedule {
+    MM_BATCH_PERSISTENT = 0, /* persistent warps take warp tiles of all views from one global queue */
+    MM_BATCH_BLOCKS = 1,     /* one launch of 16x8-pixel blocks over all views, hardware-scheduled */
+    MM_BATCH_GRAPH = 2       /* one CUDA graph of the views' own launches (each view's kernel variant) on
+                                four concurrent branches, largest views first */
+} mm_batch_schedule;
+
 typedef struct mm_batch_options {
-    int warp_tile_w;    /* pixels across one warp's 32-ray tile: 4, 8 (default), 16 or 32 */
-    int tiles_per_grab; /* warp tiles a warp takes from the shared queue at a time, 1..64 (default 4) */
+    int warp_tile_w;    /* persistent schedule: pixels across one warp's 32-ray tile: 4, 8 (default), 16, 32 */
+    int tiles_per_grab; /* persistent schedule: warp tiles taken from the queue at a time, 1..64 (default 4) */
     int use_graph;      /* 1 (default): replay a captured CUDA graph (upload, reset, kernel) */
+    int schedule;       /* mm_batch_schedule (default MM_BATCH_GRAPH, the fastest on the 70-view batch) */
 } mm_batch_options;
 
 int mm_batch_options_default(mm_batch_options* o);
 
-/* Renders n views (full frames, hardware sampler, fast math, plain cone) with the shared textures in
- * one persistent kernel: warps take tiles of all views from one queue.  The host-side records are
+/* Renders n views (full frames, hardware sampler, fast math, plain cone) with the shared textures:
+ * blocks of all views in one grid (MM_BATCH_BLOCKS; one launch per 72 views), a persistent kernel
+ * whose warps take tiles of all views from one queue (MM_BATCH_PERSISTENT), or one CUDA graph of the
+ * views' own launches on concurrent branches (MM_BATCH_GRAPH, re-captured and updated in place on
+ * every call).  The host-side records are
  * staged in pinned memory owned by the context; a call waits for the previous batch of the same
  * context to finish reading them.  The graph is re-captured when the view count or the options
  * change. */
 int mm_clouds_march_batch(mm_context ctx, const mm_view* views, int n, const mm_scene_textures* tex,
                           const mm_batch_options* opt, void* stream);
 
-/* Autotuner: times warp_tile_w in {4, 8, 16, 32} x tiles_per_grab in {1, 2, 4, 8, 16} on this batch
- * (ms_table, optional: 20 floats, row-major in that order) and returns the fastest options.
- * Synchronizes `stream`. */
+/* Autotuner: times the persistent schedule with warp_tile_w in {4, 8, 16, 32} x tiles_per_grab in
+ * {1, 2, 4, 8, 16}, the block schedule and the graph schedule on this batch (ms_table, optional:
+ * 22 floats, the 20 persistent ones row-major in that order, then blocks, then graph) and returns
+ * the fastest options.  Synchronizes `stream`. */
 int mm_batch_autotune(mm_context ctx, const mm_view* views, int n, const mm_scene_textures* tex,
                       mm_batch_options* best, float* ms_table, void* stream);
 

@@ -4,9 +4,11 @@
 // blocks, texture views, output image).  The work of all views is one queue of warp tiles (32 rays
 // each, tw x 32/tw pixels), numbered view after view; persistent warps take chunks of `grab`
 // consecutive tiles from one global counter, find the view by a binary search over the views'
-// first-tile indices, stage that view's record in shared memory and march the tile's rays exactly
-// as march_tiled_kernel does.  The record upload, the counter reset and the kernel are captured into
-// a CUDA graph once per (view count, options, textures) and replayed for later batches.
+// first-tile indices, read that view's record from constant memory and march the tile's rays
+// exactly as march_tiled_kernel does; within a view the tile rows just above its horizon come first.  The record upload, the counter reset and the kernel are captured into
+// a CUDA graph once per (view count, options, textures) and replayed for later batches.  The
+// default schedule (MM_BATCH_BLOCKS) is one ordinary launch over 16x8-pixel blocks of all views
+// instead: blocks of one SM then cover compact neighbouring tiles, as in march_tiled_kernel.
 #include <cuda_runtime.h>
 #include <stdio.h>
 #include <string.h>
@@ -81,8 +83,11 @@ __global__ void __launch_bounds__(kWarps * 32, MM_BATCH_MIN_BLOCKS) batch_kernel
             const MarchLaunch& p = c_views[v];
             const int local = tile - c_first_tile[v];
             const int tiles_x = (p.width + q.tw - 1) / q.tw;
+            // tile rows just above the view's horizon first (the long rays; see horizon_row_split)
+            const int r = local / tiles_x;
+            const int row = r < p.row_split ? p.row_split - 1 - r : r;
             const int px = (local % tiles_x) * q.tw + lane % q.tw;
-            const int py = (local / tiles_x) * th + lane / q.tw;
+            const int py = row * th + lane / q.tw;
             if (px < p.width && py < p.height) {
                 const Frame f = make_frame<false>(p);
                 Work w;
@@ -90,6 +95,34 @@ __global__ void __launch_bounds__(kWarps * 32, MM_BATCH_MIN_BLOCKS) batch_kernel
             }
         }
     }
+}
+
+// MM_BATCH_BLOCKS: one ordinary launch over the blocks of all views.  Block b belongs to the view v
+// whose first-block index is the last one <= b (c_first_tile holds block counts in this mode); the
+// block marches a 16x8-pixel tile of that view, its block rows ordered horizon-first, exactly as
+// march_tiled_kernel does for a single view, and the hardware block scheduler balances the load.
+__global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_MARCH_MIN_BLOCKS) batch_blocks_kernel(int n) {
+    __shared__ V3 s_cone[6];
+    const int b = (int)blockIdx.x;
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (c_first_tile[mid] <= b) lo = mid; else hi = mid - 1;
+    }
+    const MarchLaunch& p = c_views[lo];
+    cone_offsets(p.u, s_cone);
+    __syncthreads();
+    const int local = b - c_first_tile[lo];
+    const int blocks_x = (p.width + kBlockTileW - 1) / kBlockTileW;
+    const int r = local / blocks_x;
+    const int by = r < p.row_split ? p.row_split - 1 - r : r;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int px = (local % blocks_x) * kBlockTileW + (warp % (kBlockTileW / 8)) * 8 + (lane & 7);
+    const int py = by * kBlockTileH + (warp / (kBlockTileW / 8)) * 4 + (lane >> 3);
+    if (px >= p.width || py >= p.height) return;
+    const Frame f = make_frame<false>(p);
+    Work w;
+    march_pixel<false, MM_SAMPLER_HARDWARE>(p, f, s_cone, px, py, w);
 }
 
 }  // namespace batch
@@ -108,8 +141,71 @@ struct BatchState {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t done = nullptr;  // the last batch that read the staging buffers
-    int g_n = -1, g_tw = 0, g_grab = 0, g_grid = 0, g_launches = 0;
+    int g_n = -1, g_tw = 0, g_grab = 0, g_grid = 0, g_launches = 0, g_sched = -1;
+    // MM_BATCH_GRAPH: capture streams (one per branch) and their fork/join events
+    static constexpr int kBranches = 4;
+    cudaStream_t branch[kBranches] = {};
+    cudaEvent_t fork = nullptr, join[kBranches] = {};
 };
+
+// Views in order of decreasing ray count, dealt round-robin to the graph's branches (the longest
+// launches start first on every branch; the small ones fill the others' tails).
+int capture_views(mm_context ctx, BatchState* b, const mm_view* views, int n, const mm_scene_textures* tex,
+                  cudaGraph_t* out) {
+    constexpr int K = BatchState::kBranches;
+    if (!b->fork) {
+        MM_CUDA_TRY(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+        for (int k = 0; k < K; ++k) {
+            MM_CUDA_TRY(cudaStreamCreateWithFlags(&b->branch[k], cudaStreamNonBlocking));
+            MM_CUDA_TRY(cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming));
+        }
+    }
+    int* order = new (std::nothrow) int[n];
+    if (!order) return mm::fail(MM_ERR_OUT_OF_MEMORY, "batch: host allocation");
+    for (int i = 0; i < n; ++i) order[i] = i;
+    for (int i = 1; i < n; ++i) {  // insertion sort by decreasing pixel count (n <= 1024)
+        const int v = order[i];
+        const long long pv = (long long)views[v].out.width * views[v].out.height;
+        int j = i - 1;
+        while (j >= 0 && (long long)views[order[j]].out.width * views[order[j]].out.height < pv) {
+            order[j + 1] = order[j];
+            --j;
+        }
+        order[j + 1] = v;
+    }
+    int r = MM_OK;
+    cudaError_t e = cudaStreamBeginCapture(b->branch[0], cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        delete[] order;
+        return mm::cuda_fail(e, "batch graph capture");
+    }
+    cudaEventRecord(b->fork, b->branch[0]);
+    for (int k = 1; k < K; ++k) cudaStreamWaitEvent(b->branch[k], b->fork, 0);
+    for (int i = 0; i < n && r == MM_OK; ++i) {
+        const mm_view& v = views[order[i]];
+        mm_march_options mo;
+        mm_march_options_default(&mo);
+        mo.coverage_offset = v.coverage_offset;
+        mm::MarchLaunch p;
+        mm::fill_march_launch(v.u, tex, v.out, mo, &p);
+        r = mm::launch_march_fast(p, MM_SAMPLER_HARDWARE, MM_FORMAT_UNORM8, MM_SCHEDULE_TILED, ctx->d_work, ctx->num_sms,
+                                  b->branch[i % K]);
+    }
+    for (int k = 1; k < K; ++k) {
+        cudaEventRecord(b->join[k], b->branch[k]);
+        cudaStreamWaitEvent(b->branch[0], b->join[k], 0);
+    }
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(b->branch[0], &g);
+    delete[] order;
+    if (r == MM_OK && e != cudaSuccess) r = mm::cuda_fail(e, "batch graph capture");
+    if (r != MM_OK) {
+        if (g) cudaGraphDestroy(g);
+        return r;
+    }
+    *out = g;
+    return MM_OK;
+}
 
 BatchState* state_of(mm_context ctx) { return reinterpret_cast<BatchState*>(ctx->batch); }
 
@@ -142,7 +238,8 @@ int ensure_capacity(BatchState* b, int n) {
 
 // One launch per group of up to kViewsPerLaunch views: records to constant memory, counter reset,
 // persistent kernel.  Returns the number of launches through *launches.
-int enqueue(mm_context ctx, BatchState* b, int n, int tw, int grab, int grid, cudaStream_t s, int* launches) {
+int enqueue(mm_context ctx, BatchState* b, int n, int tw, int grab, int grid, int sched, cudaStream_t s,
+            int* launches) {
     using mm::batch::kViewsPerLaunch;
     *launches = 0;
     for (int v0 = 0; v0 < n; v0 += kViewsPerLaunch) {
@@ -152,13 +249,17 @@ int enqueue(mm_context ctx, BatchState* b, int n, int tw, int grab, int grid, cu
                                             cudaMemcpyHostToDevice, s));
         MM_CUDA_TRY(cudaMemcpyToSymbolAsync(mm::batch::c_first_tile, first, (m + 1) * sizeof(int), 0,
                                             cudaMemcpyHostToDevice, s));
-        MM_CUDA_TRY(cudaMemsetAsync(ctx->d_work + 2, 0, sizeof(unsigned int), s));
-        mm::batch::Queue q;
-        q.n = m;
-        q.tw = tw;
-        q.grab = grab;
-        q.counter = ctx->d_work + 2;
-        mm::batch::batch_kernel<<<grid, mm::batch::kWarps * 32, 0, s>>>(q);
+        if (sched == MM_BATCH_BLOCKS) {
+            mm::batch::batch_blocks_kernel<<<first[m], MM_TILED_WARPS * 32, 0, s>>>(m);
+        } else {
+            MM_CUDA_TRY(cudaMemsetAsync(ctx->d_work + 2, 0, sizeof(unsigned int), s));
+            mm::batch::Queue q;
+            q.n = m;
+            q.tw = tw;
+            q.grab = grab;
+            q.counter = ctx->d_work + 2;
+            mm::batch::batch_kernel<<<grid, mm::batch::kWarps * 32, 0, s>>>(q);
+        }
         MM_CUDA_TRY(cudaGetLastError());
         ++*launches;
     }
@@ -174,6 +275,11 @@ void batch_state_destroy(mm_context ctx) {
     drop_graph(b);
     if (b->done) cudaEventSynchronize(b->done);
     if (b->done) cudaEventDestroy(b->done);
+    for (int k = 0; k < BatchState::kBranches; ++k) {
+        if (b->branch[k]) cudaStreamDestroy(b->branch[k]);
+        if (b->join[k]) cudaEventDestroy(b->join[k]);
+    }
+    if (b->fork) cudaEventDestroy(b->fork);
     cudaFreeHost(b->h_views);
     cudaFreeHost(b->h_first);
     cudaFree(b->d_views);
@@ -189,6 +295,7 @@ extern "C" int mm_batch_options_default(mm_batch_options* o) {
     o->warp_tile_w = 8;
     o->tiles_per_grab = 4;
     o->use_graph = 1;
+    o->schedule = MM_BATCH_GRAPH;
     return MM_OK;
 }
 
@@ -206,6 +313,8 @@ extern "C" int mm_clouds_march_batch(mm_context ctx, const mm_view* views, int n
         return fail(MM_ERR_INVALID_ARGUMENT, "batch: warp_tile_w must be 4, 8, 16 or 32");
     if (o.tiles_per_grab < 1 || o.tiles_per_grab > 64)
         return fail(MM_ERR_INVALID_ARGUMENT, "batch: tiles_per_grab must be in [1, 64]");
+    if (o.schedule != MM_BATCH_BLOCKS && o.schedule != MM_BATCH_PERSISTENT && o.schedule != MM_BATCH_GRAPH)
+        return fail(MM_ERR_INVALID_ARGUMENT, "batch: bad schedule %d", o.schedule);
     // Validate textures and images as a single-view march would, through its own checks.
     for (int i = 0; i < n; ++i) {
         mm_march_options mo;
@@ -226,6 +335,36 @@ extern "C" int mm_clouds_march_batch(mm_context ctx, const mm_view* views, int n
     if (!b->done) MM_CUDA_TRY(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
     // The previous batch's upload reads the pinned staging buffers: let it finish first.
     MM_CUDA_TRY(cudaEventSynchronize(b->done));
+    if (o.schedule == MM_BATCH_GRAPH) {
+        // Each view's own launch (its kernel variant, uniforms by value) captured on the branches,
+        // then applied to the executable graph (cudaGraphExecUpdate) or instantiated anew.
+        cudaGraph_t g = nullptr;
+        int r = capture_views(ctx, b, views, n, tex, &g);
+        if (r) return r;
+        bool updated = false;
+        if (b->exec && b->g_sched == MM_BATCH_GRAPH && b->g_n == n) {
+            cudaGraphExecUpdateResultInfo info;
+            updated = cudaGraphExecUpdate(b->exec, g, &info) == cudaSuccess;
+            if (!updated) cudaGetLastError();  // clear the update failure; instantiate below
+        }
+        if (updated) {
+            cudaGraphDestroy(g);
+        } else {
+            drop_graph(b);
+            b->graph = g;
+            cudaError_t e = cudaGraphInstantiate(&b->exec, g, 0);
+            if (e != cudaSuccess) {
+                drop_graph(b);
+                return mm::cuda_fail(e, "batch graph instantiate");
+            }
+            b->g_n = n;
+            b->g_sched = MM_BATCH_GRAPH;
+        }
+        MM_CUDA_TRY(cudaGraphLaunch(b->exec, (cudaStream_t)stream));
+        mm::count_launch(n);
+        MM_CUDA_TRY(cudaEventRecord(b->done, (cudaStream_t)stream));
+        return MM_OK;
+    }
     int r = ensure_capacity(b, n);
     if (r) return r;
     const int th = 32 / o.warp_tile_w;
@@ -238,8 +377,13 @@ extern "C" int mm_clouds_march_batch(mm_context ctx, const mm_view* views, int n
             mm_march_options_default(&mo);
             mo.coverage_offset = views[i].coverage_offset;
             mm::fill_march_launch(views[i].u, tex, views[i].out, mo, &b->h_views[i]);
+            // units of the queue: 16x8-pixel blocks (MM_BATCH_BLOCKS) or warp tiles of tw x th pixels
+            const int uw = o.schedule == MM_BATCH_BLOCKS ? mm::march::kBlockTileW : o.warp_tile_w;
+            const int uh = o.schedule == MM_BATCH_BLOCKS ? mm::march::kBlockTileH : th;
+            const int unit_rows = (views[i].out.height + uh - 1) / uh;
+            b->h_views[i].row_split = mm::march::horizon_row_split(b->h_views[i], unit_rows, uh);
             first[i - v0] = total;
-            total += ((views[i].out.width + o.warp_tile_w - 1) / o.warp_tile_w) * ((views[i].out.height + th - 1) / th);
+            total += ((views[i].out.width + uw - 1) / uw) * unit_rows;
         }
         first[i - v0] = total;
     }
@@ -250,18 +394,19 @@ extern "C" int mm_clouds_march_batch(mm_context ctx, const mm_view* views, int n
     cudaStream_t s = (cudaStream_t)stream;
     int launches = 0;
     if (!o.use_graph) {
-        r = enqueue(ctx, b, n, o.warp_tile_w, o.tiles_per_grab, grid, s, &launches);
+        r = enqueue(ctx, b, n, o.warp_tile_w, o.tiles_per_grab, grid, o.schedule, s, &launches);
         if (!r) mm::count_launch(launches);
         if (!r) MM_CUDA_TRY(cudaEventRecord(b->done, s));
         return r;
     }
-    if (!b->exec || b->g_n != n || b->g_tw != o.warp_tile_w || b->g_grab != o.tiles_per_grab || b->g_grid != grid) {
+    if (!b->exec || b->g_n != n || b->g_tw != o.warp_tile_w || b->g_grab != o.tiles_per_grab || b->g_grid != grid ||
+        b->g_sched != o.schedule) {
         drop_graph(b);
         cudaStream_t cap_stream;
         MM_CUDA_TRY(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
         cudaError_t e = cudaStreamBeginCapture(cap_stream, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
-            r = enqueue(ctx, b, n, o.warp_tile_w, o.tiles_per_grab, grid, cap_stream, &launches);
+            r = enqueue(ctx, b, n, o.warp_tile_w, o.tiles_per_grab, grid, o.schedule, cap_stream, &launches);
             cudaGraph_t g = nullptr;
             cudaError_t e2 = cudaStreamEndCapture(cap_stream, &g);
             if (r == MM_OK && e2 != cudaSuccess) r = mm::cuda_fail(e2, "batch graph capture");
@@ -284,6 +429,7 @@ extern "C" int mm_clouds_march_batch(mm_context ctx, const mm_view* views, int n
         b->g_tw = o.warp_tile_w;
         b->g_grab = o.tiles_per_grab;
         b->g_grid = grid;
+        b->g_sched = o.schedule;
         b->g_launches = launches;
     }
     // The graph copies the pinned staging buffers, which hold this batch's records now.
@@ -293,7 +439,8 @@ extern "C" int mm_clouds_march_batch(mm_context ctx, const mm_view* views, int n
     return MM_OK;
 }
 
-// Times every (warp tile width, tiles per grab) pair on the given batch and returns the fastest.
+// Times every (warp tile width, tiles per grab) pair of the persistent schedule, the block schedule
+// and the graph schedule on the given batch and returns the fastest.
 extern "C" int mm_batch_autotune(mm_context ctx, const mm_view* views, int n, const mm_scene_textures* tex,
                                  mm_batch_options* best, float* ms_table, void* stream) {
     if (!best) return mm::fail(MM_ERR_INVALID_ARGUMENT, "autotune: null result");
@@ -304,12 +451,17 @@ extern "C" int mm_batch_autotune(mm_context ctx, const mm_view* views, int n, co
     MM_CUDA_TRY(cudaEventCreate(&e1));
     float best_ms = 3.4e38f;
     int r = MM_OK;
-    for (int a = 0; a < 4 && r == MM_OK; ++a)
-        for (int g = 0; g < 5 && r == MM_OK; ++g) {
+    for (int a = 0; a < 6 && r == MM_OK; ++a)
+        for (int g = 0; g < (a < 4 ? 5 : 1) && r == MM_OK; ++g) {
             mm_batch_options o;
             mm_batch_options_default(&o);
-            o.warp_tile_w = tws[a];
-            o.tiles_per_grab = grabs[g];
+            if (a < 4) {
+                o.schedule = MM_BATCH_PERSISTENT;
+                o.warp_tile_w = tws[a];
+                o.tiles_per_grab = grabs[g];
+            } else {
+                o.schedule = a == 4 ? MM_BATCH_BLOCKS : MM_BATCH_GRAPH;
+            }
             if ((r = mm_clouds_march_batch(ctx, views, n, tex, &o, stream))) break;  // warm-up and capture
             cudaEventRecord(e0, s);
             if ((r = mm_clouds_march_batch(ctx, views, n, tex, &o, stream))) break;
@@ -321,7 +473,7 @@ extern "C" int mm_batch_autotune(mm_context ctx, const mm_view* views, int n, co
             }
             float ms = 0.0f;
             cudaEventElapsedTime(&ms, e0, e1);
-            if (ms_table) ms_table[a * 5 + g] = ms;
+            if (ms_table) ms_table[a < 4 ? a * 5 + g : 20 + (a - 4)] = ms;
             if (ms < best_ms) {
                 best_ms = ms;
                 *best = o;

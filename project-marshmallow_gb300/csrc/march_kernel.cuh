@@ -793,14 +793,14 @@ __global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_LATENCY_MIN_BLOCKS) ma
 // falls monotonically down the image; the block rows whose centre ray rises are [0, split), and the
 // kernel runs them from split - 1 (the horizon) upwards before the rest.  Any other camera keeps
 // the launch order.  Only the order changes: every pixel is marched by the same code.
-inline int horizon_row_split(const MarchLaunch& p, int block_rows) {
+inline int horizon_row_split(const MarchLaunch& p, int block_rows, int rows_per_block = kBlockTileH) {
     const float* v = p.u.camera.view;
     if (v[4] != 0.0f) return 0;
     const float cpy = p.u.camera.camera_params[1];
     const bool phase16 = p.pixel_mode == MM_PIXELS_PHASE16;
     int split = 0;
     for (int r = 0; r < block_rows; ++r) {
-        const int row = r * kBlockTileH + kBlockTileH / 2;
+        const int row = r * rows_per_block + rows_per_block / 2;
         const int py = phase16 ? row * 4 + p.phase / 4 : row;
         const float spy = 2.0f * (float)py / p.uv_h - 1.0f;
         if (-v[6] - spy * cpy * v[5] > 0.0f)

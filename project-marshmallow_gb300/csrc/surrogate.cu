@@ -115,7 +115,13 @@ struct Records {
 // ------------------------------------------------------------------------------ surrogate march
 
 template <int S, bool C>
-__global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_MARCH_MIN_BLOCKS) march_sur_kernel(MarchLaunch p, Records rec) {
+// Resident blocks per SM for the surrogate march (its record writes need more registers than the
+// plain march: 9 blocks leave 56 per thread and no spills).
+#ifndef MM_SUR_MIN_BLOCKS
+#define MM_SUR_MIN_BLOCKS 9
+#endif
+
+__global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_SUR_MIN_BLOCKS) march_sur_kernel(MarchLaunch p, Records rec) {
     __shared__ V3 s_cone[6];
     cone_offsets(p.u, s_cone);
     __syncthreads();

@@ -22,6 +22,7 @@ FORMAT_UNORM8, FORMAT_FP16, FORMAT_BF16 = range(3)
 PIXELS_FULL, PIXELS_PHASE16 = range(2)
 SAMPLER_HARDWARE, SAMPLER_SOFTWARE = range(2)
 MATH_FAST, MATH_EXACT = range(2)
+BATCH_PERSISTENT, BATCH_BLOCKS, BATCH_GRAPH = range(3)
 SCHEDULE_TILED, SCHEDULE_PERSISTENT = range(2)
 CONE_PLAIN, CONE_SURROGATE = range(2)
 
@@ -92,7 +93,7 @@ class View(C.Structure):
 
 
 class BatchOptions(C.Structure):
-    _fields_ = [("warp_tile_w", C.c_int), ("tiles_per_grab", C.c_int), ("use_graph", C.c_int)]
+    _fields_ = [("warp_tile_w", C.c_int), ("tiles_per_grab", C.c_int), ("use_graph", C.c_int), ("schedule", C.c_int)]
 
 
 # Every function include/mm.h declares, with its ctypes signature.

@@ -210,7 +210,8 @@ class Renderer:
                                        out8.stride(0), C.byref(self.post_options(**opts)), _stream_ptr(stream)),
                 "mm_post_chain")
 
-    def march_batch(self, views, textures, outputs, stream=None, warp_tile_w=8, tiles_per_grab=4, use_graph=1):
+    def march_batch(self, views, textures, outputs, stream=None, warp_tile_w=8, tiles_per_grab=4, use_graph=1,
+                    schedule=L.BATCH_GRAPH):
         """views: (width, height, uniforms) triples; outputs: matching (rgba, depth) CUDA tensors."""
         arr = (L.View * len(views))()
         for i, ((w, h, u), (rgba, dep)) in enumerate(zip(views, outputs)):
@@ -218,7 +219,7 @@ class Renderer:
             arr[i].out = L.Image(rgba.data_ptr(), rgba.stride(0) * 4, dep.data_ptr() if dep is not None else None,
                                  dep.stride(0) * 4 if dep is not None else 0, w, h)
             arr[i].coverage_offset = 0.0
-        o = L.BatchOptions(warp_tile_w, tiles_per_grab, use_graph)
+        o = L.BatchOptions(warp_tile_w, tiles_per_grab, use_graph, schedule)
         st = textures.scene() if isinstance(textures, Textures) else textures
         L.check(self.lib.mm_clouds_march_batch(self.ctx, arr, len(views), C.byref(st), C.byref(o), _stream_ptr(stream)),
                 "mm_clouds_march_batch")
@@ -227,7 +228,7 @@ class Renderer:
     def autotune_batch(self, views_arr, n, textures, stream=None):
         st = textures.scene() if isinstance(textures, Textures) else textures
         best = L.BatchOptions()
-        table = (C.c_float * 20)()
+        table = (C.c_float * 22)()
         L.check(self.lib.mm_batch_autotune(self.ctx, views_arr, n, C.byref(st), C.byref(best), table,
                                            _stream_ptr(stream)), "mm_batch_autotune")
         return best, list(table)

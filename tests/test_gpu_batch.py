@@ -25,9 +25,11 @@ def test_batch_equals_single_views(cuda, env):
     views = mm.scene.cubemap_views(128) + [(320, 180, mm.scene.uniforms(320, 180, yaw=40.0, pitch=20.0)),
                                           (257, 131, mm.scene.uniforms(257, 131, yaw=200.0, pitch=8.0, time=1.0,
                                                                        sun_elevation=70.0))]
-    for tw, grab in ((8, 4), (4, 1), (32, 16)):
+    import marshmallow.lib as L
+    for tw, grab, sched in ((8, 4, L.BATCH_PERSISTENT), (4, 1, L.BATCH_PERSISTENT), (32, 16, L.BATCH_PERSISTENT),
+                            (8, 4, L.BATCH_BLOCKS), (8, 4, L.BATCH_GRAPH)):
         outs = _outputs(cuda, views)
-        r.march_batch(views, tex, outs, warp_tile_w=tw, tiles_per_grab=grab)
+        r.march_batch(views, tex, outs, warp_tile_w=tw, tiles_per_grab=grab, schedule=sched)
         cuda.cuda.synchronize()
         for (w, h, u), (rgba, dep) in zip(views, outs):
             ref = cuda.zeros((h, w, 4), device="cuda")
@@ -44,15 +46,17 @@ def test_graph_replay_takes_new_uniforms(cuda, env):
     a = [(200, 100, mm.scene.uniforms(200, 100, yaw=0.0, pitch=15.0))]
     b = [(200, 100, mm.scene.uniforms(200, 100, yaw=120.0, pitch=10.0, sun_elevation=60.0))]
     outs = _outputs(cuda, a)
-    r.march_batch(a, tex, outs)
-    first = outs[0][0].cpu().numpy()
-    r.march_batch(b, tex, outs)  # same shape and options: the captured graph is replayed
-    second = outs[0][0].cpu().numpy()
-    ref = cuda.zeros((100, 200, 4), device="cuda")
-    r.march(b[0][2], tex, ref)
-    cuda.cuda.synchronize()
-    assert not np.array_equal(first, second)
-    assert mm.metrics.frame_errors(second, ref.cpu().numpy())["rmse_255"] < 0.05
+    import marshmallow.lib as L
+    for sched in (L.BATCH_BLOCKS, L.BATCH_GRAPH, L.BATCH_PERSISTENT):
+        r.march_batch(a, tex, outs, schedule=sched)
+        first = outs[0][0].cpu().numpy()
+        r.march_batch(b, tex, outs, schedule=sched)  # same shape and options: the graph is replayed/updated
+        second = outs[0][0].cpu().numpy()
+        ref = cuda.zeros((100, 200, 4), device="cuda")
+        r.march(b[0][2], tex, ref)
+        cuda.cuda.synchronize()
+        assert not np.array_equal(first, second)
+        assert mm.metrics.frame_errors(second, ref.cpu().numpy())["rmse_255"] < 0.05
 
 
 def test_uneven_batch_and_autotune(cuda, env):
@@ -68,7 +72,8 @@ def test_uneven_batch_and_autotune(cuda, env):
     cuda.cuda.synchronize()
     ev = [cuda.cuda.Event(enable_timing=True) for _ in range(4)]
     ev[0].record()
-    r.march_batch(views, tex, outs, warp_tile_w=best.warp_tile_w, tiles_per_grab=best.tiles_per_grab)
+    r.march_batch(views, tex, outs, warp_tile_w=best.warp_tile_w, tiles_per_grab=best.tiles_per_grab,
+                  schedule=best.schedule)
     ev[1].record()
     for (w, h, u), (rgba, dep) in zip(views, outs):
         r.march(u, tex, rgba, dep)
@@ -76,10 +81,11 @@ def test_uneven_batch_and_autotune(cuda, env):
     cuda.cuda.synchronize()
     t_batch, t_seq = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
     rays = sum(w * h for w, h, _ in views)
-    print("\n70 views, %.1f Mrays: batch %.2f ms (%.0f Mrays/s, warp tile %d, grab %d) vs per-view %.2f ms"
-          % (rays / 1e6, t_batch, rays / t_batch / 1e3, best.warp_tile_w, best.tiles_per_grab, t_seq))
-    print("autotune table (ms; rows warp_tile_w 4/8/16/32, cols grab 1/2/4/8/16):")
+    print("\n70 views, %.1f Mrays: batch %.2f ms (%.0f Mrays/s, schedule %d, warp tile %d, grab %d) vs per-view %.2f ms"
+          % (rays / 1e6, t_batch, rays / t_batch / 1e3, best.schedule, best.warp_tile_w, best.tiles_per_grab, t_seq))
+    print("autotune table (ms; persistent: rows warp_tile_w 4/8/16/32, cols grab 1/2/4/8/16; then blocks):")
     for i in range(4):
         print("  " + " ".join("%8.2f" % v for v in table[5 * i:5 * i + 5]))
+    print("  blocks %8.2f   graph %8.2f" % (table[20], table[21]))
     assert best.warp_tile_w in (4, 8, 16, 32) and 1 <= best.tiles_per_grab <= 16
     assert all(v > 0 for v in table)

@@ -347,23 +347,33 @@ def reference_frame_1080p(renderer, textures, flush, stream, frames=16):
     out8 = torch.empty((H, W, 4), dtype=torch.uint8, device="cuda")
     for k in range(16):  # warm-up: fills the frame history through all 16 phases
         renderer.frame(us[k + 1], textures, bufs[k % 2], bufs[(k + 1) % 2])
+    side = torch.cuda.Stream()
+    fork, join = torch.cuda.Event(), torch.cuda.Event()
     ts = []
     for k in range(1, frames + 1):
         flush.zero_()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
         prev, cur = bufs[k % 2], bufs[(k + 1) % 2]
+        # the mesh shadow needs only the G-buffer and the textures: it runs on a second stream while
+        # the latency-bound 1/16 march runs; the post chain waits for both
+        fork.record(stream)
+        side.wait_event(fork)
+        with torch.cuda.stream(side):
+            mesh.copy_(lit)
+            renderer.mesh_shadow(us[k], textures, gbuf, rgba=mesh, stream=side)
+        join.record(side)
         renderer.frame(us[k], textures, prev, cur)
-        mesh.copy_(lit)
-        renderer.mesh_shadow(us[k], textures, gbuf, rgba=mesh)
+        stream.wait_event(join)
         renderer.post_chain(us[k], cur[0], out8, mesh=mesh)
         b.record(stream)
         torch.cuda.synchronize()
         ts.append(a.elapsed_time(b))
     ms = sum(ts) / len(ts)
     return {"ms": round(ms, 4), "fps": round(1000.0 / ms, 1), "frames": frames, "width": W, "height": H,
-            "note": "reprojection + 1/16 march + mesh cloud shadow (terrain %.0f%% of pixels) + post chain to "
-                    "8 bits; the lit mesh colour copied in from a template stands in for the mesh raster pass"
+            "note": "reprojection + 1/16 march (concurrent), mesh cloud shadow (terrain %.0f%% of pixels) on a "
+                    "second stream beside them, then the post chain to 8 bits; the lit mesh colour copied in "
+                    "from a template stands in for the mesh raster pass"
                     % (100.0 * float((gbuf[..., 3] != 0).float().mean()))}
 
 

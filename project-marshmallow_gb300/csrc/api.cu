@@ -348,6 +348,12 @@ int mm_context_destroy(mm_context c) {
     cudaFree(c->sur_y);
     cudaFree(c->sur_ray);
     mm::post_state_destroy(c);
+    if (c->aux_stream) {
+        cudaStreamSynchronize(c->aux_stream);
+        cudaStreamDestroy(c->aux_stream);
+    }
+    if (c->aux_fork) cudaEventDestroy(c->aux_fork);
+    if (c->aux_join) cudaEventDestroy(c->aux_join);
     delete c;
     return MM_OK;
 }

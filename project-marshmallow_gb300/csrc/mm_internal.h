@@ -61,6 +61,9 @@ struct mm_context_s {
     size_t post_pitch = 0;
     int post_w = 0, post_h = 0;
     cudaTextureObject_t post_gtex = 0, post_atex = 0;
+    // mm_clouds_frame: second stream for the reprojection beside the 1/16 march
+    cudaStream_t aux_stream = nullptr;
+    cudaEvent_t aux_fork = nullptr, aux_join = nullptr;
 };
 
 namespace mm {

@@ -26,6 +26,7 @@ struct P {
     float* dst_depth;
     size_t dst_depth_pitch;
     int w, h;
+    int skip_phase;  // >= 0: leave the pixels of this 1/16 phase alone (the march writes them)
 };
 
 struct v3 {
@@ -59,6 +60,7 @@ __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? l
 __global__ void __launch_bounds__(256) reproject_kernel(P p) {
     const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
     if (x >= p.w || y >= p.h) return;
+    if (p.skip_phase >= 0 && (x & 3) == (p.skip_phase & 3) && (y & 3) == (p.skip_phase >> 2)) return;
     const float* view = p.u.camera.view;
     const float* pv = p.u.camera_prev.view;
     const v3 cam = {p.u.camera.camera_position[0], p.u.camera.camera_position[1], p.u.camera.camera_position[2]};
@@ -109,11 +111,13 @@ __global__ void __launch_bounds__(256) reproject_kernel(P p) {
 }  // namespace mm
 
 namespace mm {
-int launch_reproject_fast(const mm_uniforms& u, const mm_image& src, const mm_image& dst, cudaStream_t s);
-}
+int launch_reproject_fast(const mm_uniforms& u, const mm_image& src, const mm_image& dst, int skip_phase,
+                          cudaStream_t s);
 
-extern "C" int mm_clouds_reproject(mm_context ctx, const mm_uniforms* u, const mm_image* src, const mm_image* dst,
-                                   const mm_march_options* opt, void* stream) {
+// mm_clouds_reproject with the pixels of one 1/16 phase left alone (skip_phase >= 0), for
+// mm_clouds_frame, whose march writes them.
+static int reproject(mm_context ctx, const mm_uniforms* u, const mm_image* src, const mm_image* dst,
+                     const mm_march_options* opt, int skip_phase, void* stream) {
     using mm::fail;
     if (!ctx || !u || !src || !dst) return fail(MM_ERR_INVALID_ARGUMENT, "reproject: null argument");
     const int math = opt ? opt->math : MM_MATH_FAST;
@@ -128,7 +132,7 @@ extern "C" int mm_clouds_reproject(mm_context ctx, const mm_uniforms* u, const m
     if ((src->depth && src->depth_pitch_bytes < (size_t)src->width * 4) ||
         (dst->depth && dst->depth_pitch_bytes < (size_t)dst->width * 4))
         return fail(MM_ERR_INVALID_ARGUMENT, "reproject: bad depth pitch");
-    if (math == MM_MATH_FAST) return mm::launch_reproject_fast(*u, *src, *dst, (cudaStream_t)stream);
+    if (math == MM_MATH_FAST) return mm::launch_reproject_fast(*u, *src, *dst, skip_phase, (cudaStream_t)stream);
     mm::rep::P p;
     p.u = *u;
     p.src = reinterpret_cast<const float4*>(src->rgba);
@@ -141,10 +145,17 @@ extern "C" int mm_clouds_reproject(mm_context ctx, const mm_uniforms* u, const m
     p.dst_depth_pitch = dst->depth_pitch_bytes;
     p.w = dst->width;
     p.h = dst->height;
+    p.skip_phase = skip_phase;
     mm::rep::reproject_kernel<<<dim3((p.w + 31) / 32, (p.h + 7) / 8), dim3(32, 8), 0, (cudaStream_t)stream>>>(p);
     MM_CUDA_TRY(cudaGetLastError());
     mm::count_launch();
     return MM_OK;
+}
+}  // namespace mm
+
+extern "C" int mm_clouds_reproject(mm_context ctx, const mm_uniforms* u, const mm_image* src, const mm_image* dst,
+                                   const mm_march_options* opt, void* stream) {
+    return mm::reproject(ctx, u, src, dst, opt, -1, stream);
 }
 
 extern "C" int mm_clouds_frame(mm_context ctx, const mm_uniforms* u, const mm_scene_textures* tex, const mm_image* prev,
@@ -157,6 +168,21 @@ extern "C" int mm_clouds_frame(mm_context ctx, const mm_uniforms* u, const mm_sc
     o.pixel_mode = MM_PIXELS_PHASE16;
     int r = mm::validate_march(ctx, u, tex, out, &o);
     if (r) return r;
-    if ((r = mm_clouds_reproject(ctx, u, prev, out, &o, stream))) return r;
-    return mm_clouds_march(ctx, u, tex, out, &o, stream);
+    // The march of one pixel in 16 is bounded by the latency of its longest rays and leaves most of
+    // the GPU idle; the reprojection writes the other 15 pixels in 16 (the march overwrites the
+    // phase's pixels anyway) on a second stream, concurrently.  Both read only prev and the textures.
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!ctx->aux_stream) {
+        MM_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking));
+        MM_CUDA_TRY(cudaEventCreateWithFlags(&ctx->aux_fork, cudaEventDisableTiming));
+        MM_CUDA_TRY(cudaEventCreateWithFlags(&ctx->aux_join, cudaEventDisableTiming));
+    }
+    MM_CUDA_TRY(cudaEventRecord(ctx->aux_fork, s));
+    MM_CUDA_TRY(cudaStreamWaitEvent(ctx->aux_stream, ctx->aux_fork, 0));
+    r = mm::reproject(ctx, u, prev, out, &o, (int)u->sun.color[3], ctx->aux_stream);
+    if (r == MM_OK) r = mm_clouds_march(ctx, u, tex, out, &o, stream);
+    // join in every case, so that the caller's stream never runs ahead of the reprojection
+    cudaEventRecord(ctx->aux_join, ctx->aux_stream);
+    cudaStreamWaitEvent(s, ctx->aux_join, 0);
+    return r;
 }

@@ -41,6 +41,7 @@ struct P {
     float* dst_depth;
     size_t dst_depth_pitch;
     int width, height;
+    int skip_phase;  // >= 0: leave the pixels of this 1/16 phase alone
 };
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return min(max(v, lo), hi); }
@@ -52,6 +53,7 @@ __device__ __forceinline__ float4 texel(const P& p, int x, int y) {
 __global__ void __launch_bounds__(256) reproject_fast_kernel(P p) {
     const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
     if (x >= p.width || y >= p.height) return;
+    if (p.skip_phase >= 0 && (x & 3) == (p.skip_phase & 3) && (y & 3) == (p.skip_phase >> 2)) return;
     const float sx = fmaf((float)x, p.sxs, -1.0f), sy = fmaf((float)y, p.sys, -1.0f);
     float dx = p.ax + sx * p.rx - sy * p.ux;
     float dy = p.ay + sx * p.ry - sy * p.uy;
@@ -109,7 +111,8 @@ __global__ void __launch_bounds__(256) reproject_fast_kernel(P p) {
 }  // namespace repf
 
 // Host side: the per-frame terms, then the launch.  src/dst validated by the caller.
-int launch_reproject_fast(const mm_uniforms& u, const mm_image& src, const mm_image& dst, cudaStream_t s) {
+int launch_reproject_fast(const mm_uniforms& u, const mm_image& src, const mm_image& dst, int skip_phase,
+                          cudaStream_t s) {
     repf::P p;
     const float* v = u.camera.view;
     const float* pv = u.camera_prev.view;
@@ -149,6 +152,7 @@ int launch_reproject_fast(const mm_uniforms& u, const mm_image& src, const mm_im
     p.dst_depth_pitch = dst.depth_pitch_bytes;
     p.width = dst.width;
     p.height = dst.height;
+    p.skip_phase = skip_phase;
     repf::reproject_fast_kernel<<<dim3((p.width + 31) / 32, (p.height + 7) / 8), dim3(32, 8), 0, s>>>(p);
     MM_CUDA_TRY(cudaGetLastError());
     count_launch();

@@ -93,3 +93,26 @@ def test_reproject_fast_matches_exact(cuda, env, frame):
     # one tap in ~2000 lands within rounding of a pixel boundary (the centre tap: 0.055% measured);
     # with ten taps per pixel that moves ~0.5% of the pixels
     assert close.mean() >= 0.99 and same_centre.mean() >= 0.999
+
+
+@pytest.mark.parametrize("math", [0, 1])
+def test_frame_equals_sequential_passes(cuda, env, math):
+    # mm_clouds_frame runs the reprojection of the other 15 pixels in 16 on a second stream beside
+    # the 1/16 march: the result equals reprojecting every pixel and then marching the phase.
+    import marshmallow as mm
+    tex, r = env
+    w, h = 333, 190
+    for k, phase in ((3, 0), (4, 6), (5, 15)):
+        u = mm.scene.sweep_uniforms(k, w, h)
+        u.camera_prev = mm.scene.sweep_uniforms(k - 1, w, h).camera_prev
+        u.sun.color[3] = float(phase)
+        rng = np.random.default_rng(k)
+        prev = (cuda.from_numpy(rng.uniform(0, 3, (h, w, 4)).astype(np.float32)).cuda(),
+                cuda.from_numpy(rng.uniform(1e3, 1e5, (h, w)).astype(np.float32)).cuda())
+        a = (cuda.full((h, w, 4), -1.0, device="cuda"), cuda.full((h, w), -1.0, device="cuda"))
+        b = (cuda.full((h, w, 4), -1.0, device="cuda"), cuda.full((h, w), -1.0, device="cuda"))
+        r.frame(u, tex, prev, a, math=math)
+        r.reproject(u, prev, b, math=math)
+        r.march(u, tex, b[0], b[1], pixel_mode=1, math=math)
+        cuda.cuda.synchronize()
+        assert cuda.equal(a[0], b[0]) and cuda.equal(a[1], b[1]), (k, phase)

@@ -6,7 +6,7 @@
  *
  *  - oracle_march_*: a line-by-line restatement of SkyEngine/SkyEngine/Shaders/compute-clouds.comp
  *    (:65-500) in C++, instantiated in float (the FP32 parity twin and the timed CPU baseline) and
- *    in double (the FP64 error judge), with software samplers that implement the reference
+ *    in double (the FP64 yardstick for errors), with software samplers that implement the reference
  *    samplers (LINEAR, REPEAT, normalized coordinates, mip 0; Texture.cpp:29-52, 315-338).
  *  - oracle_ref_curl: a restatement of SkyEngine/SkyEngine/ImageUtils.cpp:25-222
  *    (GenerateCurlNoise), pinned against the shipped Textures/CurlNoiseFBM.tga.

@@ -2,7 +2,7 @@
 //
 // Follows SkyEngine/SkyEngine/Shaders/compute-clouds.comp line by line; each function names the
 // lines it restates.  The template runs in float (T = float: the FP32 parity twin of the CUDA
-// kernel and the timed CPU baseline) and in double (T = double: the error judge).
+// kernel and the timed CPU baseline) and in double (T = double: the yardstick for errors).
 //
 // Arithmetic conventions (these fix the evaluation order the GLSL source leaves to the compiler):
 //  - expressions are evaluated left to right as written, no contraction into fused multiply-add

@@ -495,6 +495,13 @@ int mm_measure_peaks(mm_texture tex3d, mm_texture tex2d, double* out, void* stre
 int mm_tc_gemm_check(const void* d_a, const void* d_b, int K, int N, int variant, float* d_out, int* d_status,
                      void* stream);
 
+/* Self-test of the bounded mbarrier wait every tensor-core kernel uses: one thread initializes an
+ * mbarrier, arrives on it (arrive != 0) or not, and waits for its phase for at most poll_limit polls
+ * (1 .. 2^24).  *d_status becomes 0 if the phase completed and 1 if the wait gave up — the path a
+ * kernel takes when an expected arrival never comes: it reports and returns instead of hanging.
+ * No reference counterpart. */
+int mm_tc_wait_check(int arrive, unsigned int poll_limit, int* d_status, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

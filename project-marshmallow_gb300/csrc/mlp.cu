@@ -772,3 +772,29 @@ extern "C" int mm_tc_gemm_check(const void* d_a, const void* d_b, int K, int N, 
     count_launch();
     return MM_OK;
 }
+
+// ------------------------------------------------------------------------------ bounded-wait self-test
+
+namespace {
+
+// One thread initializes an mbarrier (arrival count 1), arrives on it or not, and waits for its
+// phase with a poll limit: status 0 = the phase completed, 1 = the wait gave up (nothing arrived).
+__global__ void wait_check_kernel(int arrive, unsigned int limit, int* status) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x != 0) return;
+    mm::tc::mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    if (arrive) mm::tc::mbar_arrive(&bar);
+    *status = mm::tc::mbar_wait(&bar, 0, limit) ? 0 : 1;
+}
+
+}  // namespace
+
+extern "C" int mm_tc_wait_check(int arrive, unsigned int poll_limit, int* d_status, void* stream) {
+    if (!d_status || poll_limit == 0 || poll_limit > (1u << 24))
+        return mm::fail(MM_ERR_INVALID_ARGUMENT, "wait check: bad arguments");
+    wait_check_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(arrive ? 1 : 0, poll_limit, d_status);
+    MM_CUDA_TRY(cudaGetLastError());
+    mm::count_launch();
+    return MM_OK;
+}

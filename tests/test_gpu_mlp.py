@@ -117,3 +117,17 @@ def test_training_reduces_loss_and_checkpoints(cuda, mmlib, tmp_path):
         assert mmlib.mm_mlp_load(h, bad.encode()) == 1
     finally:
         mmlib.mm_mlp_destroy(h)
+
+
+def test_bounded_wait_gives_up_and_reports(cuda, mmlib):
+    # The tensor-core kernels wait on mbarriers with a poll limit.  An arrival that never comes (a
+    # barrier nothing arrives on) makes the wait give up and report instead of hanging the GPU; the
+    # context stays usable afterwards.
+    import ctypes as C
+    st = cuda.full((2,), -1, dtype=cuda.int32, device="cuda")
+    assert mmlib.mm_tc_wait_check(1, 4096, C.c_void_p(st.data_ptr()), None) == 0
+    assert mmlib.mm_tc_wait_check(0, 4096, C.c_void_p(st.data_ptr() + 4), None) == 0
+    cuda.cuda.synchronize()
+    assert st.cpu().tolist() == [0, 1]
+    x = cuda.ones(1024, device="cuda")
+    assert float((x * 2).sum()) == 2048.0

@@ -262,8 +262,10 @@ typedef enum mm_math_mode {
 
 typedef enum mm_schedule {
     MM_SCHEDULE_TILED = 0,      /* one thread marches one pixel start to end (the shader's own loop
-                                   nest), 8x4 pixel tiles per warp, the six sun-cone taps of a sample
-                                   fetched together */
+                                   nest), 8x4 pixel tiles per warp, block rows just above the horizon
+                                   first; the sun-cone taps of a sample are fetched one at a time in
+                                   full frames, in pairs in large 1/16-pixel launches and all six
+                                   together in launches of <= 262144 rays (latency-bound) */
     MM_SCHEDULE_PERSISTENT = 1  /* persistent warps; each iteration evaluates one cloudTest per lane
                                    (a march step or a sun-cone tap); finished lanes take the next ray
                                    of their warp's 8x4 pixel tile (ballot compaction).  Full SIMT
@@ -272,9 +274,11 @@ typedef enum mm_schedule {
 
 typedef enum mm_cone_mode {
     MM_CONE_PLAIN = 0,     /* the six-tap sun cone of compute-clouds.comp:441-453 */
-    MM_CONE_SURROGATE = 1  /* two cone taps + the trained MLP (mm_march_options.surrogate) predict
-                              Beer's transmittance of the six-tap sum; full frames, hardware
-                              sampler, fast math and the tiled schedule only */
+    MM_CONE_SURROGATE = 1  /* the cone taps' low-res densities + the trained MLP
+                              (mm_march_options.surrogate) predict Beer's transmittance of the
+                              six-tap sum; full frames, hardware sampler, fast math and the tiled
+                              schedule only.  Frames with the sun below the horizon lie outside the
+                              training envelope (elevations 0-90 degrees) and take the plain cone */
 } mm_cone_mode;
 
 typedef struct mm_march_options {

@@ -516,7 +516,10 @@ int mm_clouds_march(mm_context ctx, const mm_uniforms* u, const mm_scene_texture
     mm::MarchLaunch p;
     mm::fill_march_launch(*u, tex, *out, o, &p);
     cudaStream_t s = (cudaStream_t)stream;
-    if (o.cone == MM_CONE_SURROGATE) return mm::launch_surrogate_frame(p, ctx, o.surrogate, s);
+    // The surrogate was trained on sun elevations 0-90 degrees (mm_surrogate_generate); with the sun
+    // below the horizon a frame is outside that envelope and takes the plain cone march.
+    if (o.cone == MM_CONE_SURROGATE && u->sun.direction[1] >= 0.0f)
+        return mm::launch_surrogate_frame(p, ctx, o.surrogate, s);
     if (o.math == MM_MATH_EXACT) return mm::launch_march_exact(p, o.sampler, o.schedule, ctx->d_work, ctx->num_sms, s);
     return mm::launch_march_fast(p, o.sampler, o.density_format, o.schedule, ctx->d_work, ctx->num_sms, s);
 }

@@ -98,3 +98,31 @@ def test_surrogate_frames_vs_plain_and_oracle(cuda, mmlib, orc, trained):
     finally:
         r.close()
         tex.close()
+
+
+def test_night_frames_fall_back_to_the_plain_cone(cuda, mmlib, trained):
+    # Outside the training envelope (sun below the horizon) a surrogate request marches the plain
+    # cone: the frame equals the plain march bit for bit.
+    import marshmallow as mm
+    import marshmallow.lib as L
+    net = trained[0] if isinstance(trained, tuple) else trained
+    w, h = 320, 180
+    u = mm.scene.uniforms(w, h, yaw=30.0, pitch=12.0, sun_elevation=-6.0)
+    rng = np.random.default_rng(3)
+    night = rng.integers(0, 256, (64, 128, 4), dtype=np.uint8)
+    tex = mm.render.Textures(seed=0)
+    nt = mm.render.Textures.from_arrays({"night_sky": night})
+    tex.handles["night_sky"] = nt.handles["night_sky"]
+    r = mm.render.Renderer()
+    try:
+        a = cuda.zeros((h, w, 4), device="cuda")
+        b = cuda.zeros((h, w, 4), device="cuda")
+        r.march(u, tex, a, surrogate=net)
+        r.march(u, tex, b)
+        cuda.cuda.synchronize()
+        assert cuda.equal(a, b)
+    finally:
+        r.close()
+        del tex.handles["night_sky"]
+        tex.close()
+        nt.close()

@@ -323,6 +323,42 @@ def measure_passes(renderer, textures, rgba, depth, uniforms, w, h, flush, strea
     return out
 
 
+def measure_configs(renderer, textures, flush, stream, with_cpu):
+    """The two smaller workloads of the baseline plan, GPU beside the CPU restatement: the 256x256
+    camera (pitch 15 deg, sun 30 deg, t = 0) and the 1920x1080 16-frame sweep; production arithmetic,
+    hardware sampler, full frames.  CPU: the FP32 oracle on all host threads, the whole 256x256 frame
+    and every 2nd row and column of the 16 sweep frames."""
+    import torch
+    import marshmallow as mm
+    out = {}
+    u0 = mm.scene.uniforms(256, 256)
+    rgba = torch.empty((256, 256, 4), device="cuda")
+    dep = torch.empty((256, 256), device="cuda")
+    ms0 = _median_ms(lambda: renderer.march(u0, textures, rgba, dep), flush, stream)
+    out["camera_256"] = {"ms": round(ms0, 4), "mrays_per_s": round(256 * 256 / ms0 / 1e3, 1)}
+    W, H = 1920, 1080
+    rgba = torch.empty((H, W, 4), device="cuda")
+    dep = torch.empty((H, W), device="cuda")
+    us = [mm.scene.sweep_uniforms(k, W, H) for k in range(SWEEP)]
+    ms1 = sum(_median_ms(lambda: renderer.march(u, textures, rgba, dep), flush, stream, n=3) for u in us) / SWEEP
+    out["sweep_1080p"] = {"ms_per_frame": round(ms1, 4), "mrays_per_s": round(W * H / ms1 / 1e3, 1)}
+    if with_cpu:
+        host = textures.host_all()
+        n, dt, th = cpu_march_sample(u0, host, 256, 256, 0, 1)
+        out["camera_256"]["cpu"] = {"ms": round(1e3 * dt, 2), "mrays_per_s": round(n / dt / 1e6, 3), "cores": th,
+                                    "kind": "port"}
+        rays = 0
+        secs = 0.0
+        for k, u in enumerate(us):
+            n, dt, th = cpu_march_sample(u, host, W, H, k % 2, 2)
+            rays += n
+            secs += dt
+        out["sweep_1080p"]["cpu"] = {"mrays_per_s": round(rays / secs / 1e6, 3), "cores": th, "kind": "port",
+                                     "ms_per_frame_estimated": round(1e3 * secs / SWEEP * (W * H * SWEEP / rays), 1),
+                                     "sample": "every 2nd row and column of the 16 frames (%.1f s)" % secs}
+    return out
+
+
 def reference_frame_1080p(renderer, textures, flush, stream, frames=16):
     """The reference application's per-frame GPU work at its own resolution (1920x1080), as this
     library runs it: mm_clouds_frame (reprojection of every pixel + the march of one pixel in 16),
@@ -548,6 +584,10 @@ def run_ours(args):
                "sample": "FP32 oracle restatement of compute-clouds.comp on the 16 sweep frames, every 3rd row "
                          "and column (%d rays, %.1f s)" % (rays, secs)}
 
+    configs = None
+    if rank == 0 and world == 1 and not args.no_passes:
+        configs = measure_configs(renderer, textures, flush, stream, not args.no_cpu_baseline)
+
     passes = None
     if rank == 0 and not args.no_passes:
         passes = measure_passes(renderer, textures, rgba, depth, uniforms, w, h, flush, stream, hbm_peak,
@@ -580,7 +620,7 @@ def run_ours(args):
             "work_per_frame": {"cloud_test": n_test / args.steps, "cloud_hires": n_hires / args.steps,
                                "iterations": n_iter / args.steps, "accumulated": n_acc / args.steps},
             "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks, "cpu_baseline": cpu,
-            "passes": passes,
+            "configs": configs, "passes": passes,
         }
         print(json.dumps(line), flush=True)
     renderer.close()

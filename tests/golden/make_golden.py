@@ -9,6 +9,9 @@
                       setTime (SkyManager.cpp, compiled by `make -C oracle ref`).
   nubis_stats.json    mean / deviation of the shipped Nubis density textures (the targets of the
                       seeded generators' output maps).
+  camera_reference.json  view/projection/aspect/tanHalfFov of the reference Camera (camera.cpp,
+                      compiled by `make -C oracle ref` with forwarding headers for its Windows-style
+                      includes) for a set of poses, frusta and image sizes.
   asset_digests.json  SHA-256 of the RGBA8 decode (stbi_load(..., STBI_rgb_alpha) conventions) of the
                       shipped textures the reference loads, from the independent decoders in
                       tests/tga.py and tests/png.py; the library's loader must reproduce them.
@@ -97,6 +100,16 @@ def main():
     inp = "".join("%.9g %.9g %.9g\n" % t for t in triples)
     out = subprocess.run([os.path.join(bins, "ref_sky")], input=inp, capture_output=True, text=True, check=True).stdout
     with open(os.path.join(HERE, "sky_reference.json"), "w") as f:
+        json.dump(json.loads(out), f, indent=0)
+
+    poses = []
+    for (eye, fov, w, h) in (((0.0, 10.0, 0.0), 60.0, 256, 256), ((0.0, 10.0, 0.0), 60.0, 1920, 1080),
+                             ((5.0, 150.0, -3.0), 45.0, 3840, 2160), ((1000.0, 300.0, -2000.0), 90.0, 512, 512)):
+        for yaw, pitch in ((0.0, 15.0), (30.0, 5.0), (90.0, 25.0), (200.0, 40.0), (270.0, 0.0), (359.0, 89.9)):
+            poses.append("%g %g %g %g %g %g %d %d\n" % (eye + (yaw, pitch, fov, w, h)))
+    out = subprocess.run([os.path.join(bins, "ref_camera")], input="".join(poses), capture_output=True, text=True,
+                         check=True).stdout
+    with open(os.path.join(HERE, "camera_reference.json"), "w") as f:
         json.dump(json.loads(out), f, indent=0)
 
     d3 = os.path.join(se, "Textures", "3DTextures")

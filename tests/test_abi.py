@@ -82,3 +82,31 @@ def test_camera_basis(mmlib):
     np.testing.assert_allclose(-fwd, [math.cos(y) * math.cos(p), math.sin(p), math.sin(y) * math.cos(p)], atol=1e-6)
     assert abs(u.camera.camera_params[0] - 1920 / 1080) < 1e-6
     assert abs(u.camera.camera_params[1] - math.tan(0.5 * 0.01745 * 60)) < 1e-6
+
+
+def test_camera_matches_reference_camera(mmlib):
+    # tests/golden/camera_reference.json: the reference's own Camera (camera.cpp compiled unchanged)
+    # built as the application builds it (near 0.1, far 1000) and pointed by lookAt at (yaw, pitch);
+    # its m_forward is the reverse of the direction the image centre looks at, so the same camera is
+    # mm_camera_from_angles(eye, yaw + 180, -pitch).  View and projection agree to float rounding.
+    import ctypes as C
+    import json
+    import os
+
+    import numpy as np
+
+    import marshmallow.lib as L
+    from conftest import GOLDEN
+    recs = json.load(open(os.path.join(GOLDEN, "camera_reference.json")))
+    assert len(recs) == 24
+    for rec in recs:
+        u = L.Uniforms()
+        e = (C.c_float * 3)(*rec["eye"])
+        L.check(mmlib.mm_camera_from_angles(e, rec["yaw"] + 180.0, -rec["pitch"], rec["fov"], rec["width"],
+                                            rec["height"], C.byref(u)))
+        v, rv = np.array(u.camera.view[:]), np.array(rec["view"])
+        p, rp = np.array(u.camera.proj[:]), np.array(rec["proj"])
+        assert np.abs(v - rv).max() <= 1e-6 * max(1.0, np.abs(rv).max()), rec
+        assert np.abs(p - rp).max() <= 1e-6 * np.abs(rp).max(), rec
+        assert abs(u.camera.camera_params[0] - rec["aspect"][0]) <= 1e-7 * rec["aspect"][0]
+        assert abs(u.camera.camera_params[1] - rec["tan_half_fov"][0]) <= 1e-7 * rec["tan_half_fov"][0]

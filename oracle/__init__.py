@@ -132,6 +132,35 @@ def _textures(textures):
     return keep, t
 
 
+REF_CLOUDS_LIB = os.path.join(ORACLE_DIR, "_ref", "libref_clouds.so")
+_ref_clouds = None
+
+
+def ref_clouds_available():
+    """True where the reference's compute-clouds.comp has been compiled as C++ (`make -C oracle ref`)."""
+    return os.path.exists(REF_CLOUDS_LIB)
+
+
+def ref_clouds_march(uniforms, textures, xs, ys, nthreads=0):
+    """The reference shader itself (compiled from its GLSL on the CPU) at pixels (xs[i], ys[i]) of the
+    1920 x 1080 frame it hard-codes; every pixel must be in the phase int(sun.color.a).  Returns rgba (n, 4)."""
+    global _ref_clouds
+    if _ref_clouds is None:
+        lib = C.CDLL(REF_CLOUDS_LIB)
+        lib.ref_clouds_march.argtypes = [C.c_void_p, C.POINTER(OracleTextures), C.c_void_p, C.c_void_p, C.c_size_t,
+                                         C.c_void_p, C.c_int]
+        _ref_clouds = lib
+    keep, t = _textures(textures)
+    xs = np.ascontiguousarray(xs, np.int32)
+    ys = np.ascontiguousarray(ys, np.int32)
+    out = np.zeros((len(xs), 4), np.float32)
+    rc = _ref_clouds.ref_clouds_march(C.addressof(uniforms), C.byref(t), xs.ctypes.data, ys.ctypes.data, len(xs),
+                                      out.ctypes.data, nthreads)
+    if rc:
+        raise RuntimeError("ref_clouds_march failed: %d" % rc)
+    return out
+
+
 def shadow(uniforms, textures, world_pos, precision=32, coverage_offset=0.0, nthreads=0):
     """model.frag's cloud-shadow march over a G-buffer of world positions (..., 4) -> shadow (...)."""
     lib = load()

@@ -1,0 +1,133 @@
+// glsl_shim.h - lets the reference's GLSL shaders compile unchanged as C++ on glm (test
+// infrastructure: builds the checker's reference, never the library).
+//
+// oracle/ref/glsl_to_cpp.py turns a shader into a C++ translation unit: it drops the three lines
+// that are GLSL-only syntax (#version, #extension, precision), marks decimal literals as float
+// (GLSL literals are single precision, C++ ones double) and includes this header first.  Everything
+// else is the shader's own text:
+//  - layout(...) qualifiers vanish; `uniform` becomes `struct`, so a uniform block
+//    `uniform Camera { ... } camera;` declares a global struct and `uniform sampler2D s;` a global of
+//    the sampler type below; `in`/`out` varyings become globals (thread_local: one invocation per
+//    host thread at a time); `in`/`inout` parameter qualifiers vanish (the shaders read their
+//    inout parameters back nowhere);
+//  - vec/mat types and the built-in functions are glm's (swizzles included), with float overloads
+//    for the calls GLSL makes with integer literals (clamp(x, 0, 1) and the like);
+//  - samplers: LINEAR filter with float weights, REPEAT or CLAMP_TO_EDGE, mip 0, on UNORM8 or float
+//    texels — the definition shared with the CPU restatement (x = u*N - 0.5, i0 = floor(x),
+//    a = x - i0, interpolated along x, then y, then z);
+//  - images: imageStore / imageLoad / imageSize on float4 rows;
+//  - main() is renamed glsl_main(); gl_GlobalInvocationID is a thread_local the driver sets.
+#pragma once
+
+#define GLM_FORCE_SWIZZLE
+#include <glm/glm.hpp>
+
+#include <cmath>
+#include <cstdint>
+
+using namespace glm;
+
+#define layout(...)
+#define uniform struct
+#define readonly
+#define writeonly
+#define highp
+#define in
+#define inout
+#define out
+#define main glsl_main
+
+// ---------------------------------------------------------------------------------- built-ins
+
+thread_local uvec3 gl_GlobalInvocationID;
+
+inline float clamp(float x, float a, float b) { return glm::clamp(x, a, b); }
+inline float min(float a, float b) { return glm::min(a, b); }
+inline float max(float a, float b) { return glm::max(a, b); }
+inline float mix(float a, float b, float t) { return glm::mix(a, b, t); }
+inline float smoothstep(float e0, float e1, float x) { return glm::smoothstep(e0, e1, x); }
+
+// ---------------------------------------------------------------------------------- samplers
+
+struct GlslSampler {
+    const void* texels = nullptr;  // UNORM8 (bytes) or float texels, x fastest, then y, then z
+    int w = 1, h = 1, d = 1, channels = 4;
+    bool is_float = false;         // float texels (framebuffers) instead of UNORM8
+    bool clamp_edge = false;       // CLAMP_TO_EDGE instead of REPEAT
+    vec4 fetch(int x, int y, int z) const {
+        if (clamp_edge) {
+            x = x < 0 ? 0 : (x >= w ? w - 1 : x);
+            y = y < 0 ? 0 : (y >= h ? h - 1 : y);
+            z = z < 0 ? 0 : (z >= d ? d - 1 : z);
+        } else {
+            x %= w;
+            x += x < 0 ? w : 0;
+            y %= h;
+            y += y < 0 ? h : 0;
+            z %= d;
+            z += z < 0 ? d : 0;
+        }
+        const size_t i = (((size_t)z * h + y) * w + x) * channels;
+        float v[4] = {0.0f, 0.0f, 0.0f, 1.0f};
+        for (int c = 0; c < channels && c < 4; ++c)
+            v[c] = is_float ? static_cast<const float*>(texels)[i + c]
+                            : (float)static_cast<const uint8_t*>(texels)[i + c] / 255.0f;
+        return vec4(v[0], v[1], v[2], v[3]);
+    }
+};
+struct sampler2D : GlslSampler {};
+struct sampler3D : GlslSampler {};
+
+inline vec4 mix4(const vec4& a, const vec4& b, float t) {
+    return vec4(a.x * (1.0f - t) + b.x * t, a.y * (1.0f - t) + b.y * t, a.z * (1.0f - t) + b.z * t,
+                a.w * (1.0f - t) + b.w * t);
+}
+
+inline vec4 texture(const sampler2D& s, vec2 uv) {
+    const float x = uv.x * (float)s.w - 0.5f, y = uv.y * (float)s.h - 0.5f;
+    const float fx = std::floor(x), fy = std::floor(y);
+    const float ax = x - fx, ay = y - fy;
+    // CLAMP_TO_EDGE may clamp the base texel first (it keeps far coordinates out of int overflow);
+    // REPEAT wraps the true floor
+    const int x0 = s.clamp_edge ? (int)fminf(fmaxf(fx, -2.0f), (float)s.w + 1.0f) : (int)fx;
+    const int y0 = s.clamp_edge ? (int)fminf(fmaxf(fy, -2.0f), (float)s.h + 1.0f) : (int)fy;
+    const vec4 a = mix4(s.fetch(x0, y0, 0), s.fetch(x0 + 1, y0, 0), ax);
+    const vec4 b = mix4(s.fetch(x0, y0 + 1, 0), s.fetch(x0 + 1, y0 + 1, 0), ax);
+    return mix4(a, b, ay);
+}
+
+inline vec4 texture(const sampler3D& s, vec3 p) {
+    const float x = p.x * (float)s.w - 0.5f, y = p.y * (float)s.h - 0.5f, z = p.z * (float)s.d - 0.5f;
+    const float fx = std::floor(x), fy = std::floor(y), fz = std::floor(z);
+    const float ax = x - fx, ay = y - fy, az = z - fz;
+    const int x0 = (int)fx, y0 = (int)fy, z0 = (int)fz;
+    const vec4 a = mix4(s.fetch(x0, y0, z0), s.fetch(x0 + 1, y0, z0), ax);
+    const vec4 b = mix4(s.fetch(x0, y0 + 1, z0), s.fetch(x0 + 1, y0 + 1, z0), ax);
+    const vec4 c = mix4(s.fetch(x0, y0, z0 + 1), s.fetch(x0 + 1, y0, z0 + 1), ax);
+    const vec4 e = mix4(s.fetch(x0, y0 + 1, z0 + 1), s.fetch(x0 + 1, y0 + 1, z0 + 1), ax);
+    return mix4(mix4(a, b, ay), mix4(c, e, ay), az);
+}
+
+// ---------------------------------------------------------------------------------- images
+
+struct image2D {
+    float* texels = nullptr;  // float4 rows
+    int w = 0, h = 0;
+};
+
+inline void imageStore(image2D& im, ivec2 p, vec4 v) {
+    if (p.x < 0 || p.y < 0 || p.x >= im.w || p.y >= im.h) return;
+    float* t = im.texels + ((size_t)p.y * im.w + p.x) * 4;
+    t[0] = v.x;
+    t[1] = v.y;
+    t[2] = v.z;
+    t[3] = v.w;
+}
+
+inline vec4 imageLoad(const image2D& im, ivec2 p) {
+    if (p.x < 0 || p.y < 0 || p.x >= im.w || p.y >= im.h) return vec4(0.0f);
+    const float* t = im.texels + ((size_t)p.y * im.w + p.x) * 4;
+    return vec4(t[0], t[1], t[2], t[3]);
+}
+
+inline ivec2 imageSize(const image2D& im) { return ivec2(im.w, im.h); }

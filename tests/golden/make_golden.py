@@ -12,11 +12,16 @@
   camera_reference.json  view/projection/aspect/tanHalfFov of the reference Camera (camera.cpp,
                       compiled by `make -C oracle ref` with forwarding headers for its Windows-style
                       includes) for a set of poses, frusta and image sizes.
+  shader_clouds_1080p.npz  the reference's own compute-clouds.comp, compiled unchanged as C++ on the
+                      CPU (`make -C oracle ref`: oracle/ref/glsl_to_cpp.py + glsl_shim.h), on the
+                      seed-0 generator textures: for five frames (sweep poses, a low sun, a night sky;
+                      pixel phases 0, 5, 10, 15, 3) the rgba of every 32nd pixel of the phase in x and y
+                      of its hard-coded 1920x1080 frame, with the uniform blocks that made them.
   asset_digests.json  SHA-256 of the RGBA8 decode (stbi_load(..., STBI_rgb_alpha) conventions) of the
                       shipped textures the reference loads, from the independent decoders in
                       tests/tga.py and tests/png.py; the library's loader must reproduce them.
 
-Usage: python tests/golden/make_golden.py [REFERENCE_ROOT] [--digests-only]
+Usage: python tests/golden/make_golden.py [REFERENCE_ROOT] [--digests-only | --shader-only]
 
 """
 import json
@@ -69,6 +74,57 @@ def asset_digests(se):
         json.dump(d, f, indent=1)
 
 
+SHADER_STRIDE = 32
+
+
+def shader_frames():
+    """(name, uniforms, night-sky texels or None) of the compute-clouds.comp golden frames."""
+    sys.path.insert(0, os.path.join(REPO, "project-marshmallow_gb300"))
+    sys.path.insert(0, REPO)
+    import marshmallow as mm
+    import marshmallow.lib as L
+    import oracle
+    night = oracle.noise(L.NOISE_WEATHER, 3, 160, 90, 1, 4)[0]
+    frames = [("sweep0", mm.scene.sweep_uniforms(0, 1920, 1080), 0),
+              ("sweep7", mm.scene.sweep_uniforms(7, 1920, 1080), 5),
+              ("sweep12", mm.scene.sweep_uniforms(12, 1920, 1080), 10),
+              ("low_sun", mm.scene.uniforms(1920, 1080, yaw=120.0, pitch=4.0, sun_elevation=3.0, time=40.0), 15),
+              ("night", mm.scene.uniforms(1920, 1080, yaw=300.0, pitch=9.0, sun_elevation=-12.0), 3)]
+    out = []
+    for name, u, phase in frames:
+        u.sun.color[3] = float(phase)
+        out.append((name, u, night if u.sun.direction[1] < 0 else None))
+    return out
+
+
+def shader_pixels(phase, stride=SHADER_STRIDE):
+    """Row and column lists of the golden pixels of a phase: every stride-th pixel of the phase."""
+    return np.arange(phase // 4, 1080, stride), np.arange(phase % 4, 1920, stride)
+
+
+def shader_clouds_golden():
+    import ctypes as C
+    sys.path.insert(0, os.path.join(REPO, "project-marshmallow_gb300"))
+    sys.path.insert(0, REPO)
+    import oracle
+    import marshmallow.lib as L
+    tex = {"low_res": oracle.noise(L.NOISE_LOWRES, 0, 128, 128, 128, 4),
+           "hi_res": oracle.noise(L.NOISE_HIRES, 0, 32, 32, 32, 4),
+           "curl": oracle.noise(L.NOISE_CURL2D, 0, 128, 128, 1, 2)[0],
+           "weather": oracle.noise(L.NOISE_WEATHER, 0, 512, 512, 1, 4)[0]}
+    names, ublocks, images = [], [], []
+    for name, u, night in shader_frames():
+        t = dict(tex, night_sky=night)
+        rows, cols = shader_pixels(int(u.sun.color[3]))
+        ys, xs = np.meshgrid(rows, cols, indexing="ij")
+        rgba = oracle.ref_clouds_march(u, t, xs.ravel(), ys.ravel()).reshape(len(rows), len(cols), 4)
+        names.append(name)
+        ublocks.append(np.frombuffer(C.string_at(C.addressof(u), C.sizeof(u)), np.uint8))
+        images.append(rgba)
+    np.savez_compressed(os.path.join(HERE, "shader_clouds_1080p.npz"), names=np.array(names),
+                        uniforms=np.stack(ublocks), rgba=np.stack(images), stride=SHADER_STRIDE)
+
+
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     ref = args[0] if args else "/root/reference"
@@ -78,6 +134,9 @@ def main():
         return
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", "REF=" + ref], check=True)
     bins = os.path.join(REPO, "oracle", "_ref")
+    shader_clouds_golden()
+    if "--shader-only" in sys.argv:
+        return
 
     shipped = read_tga(os.path.join(se, "Textures", "CurlNoiseFBM.tga"))
     tmp = os.path.join(bins, "curl_from_reference.tga")

@@ -168,6 +168,34 @@ def test_reference_uv_mode(cuda, orc, renderer, gpu_textures, host_textures):
     assert np.array_equal(rgba, ref)
 
 
+@pytest.mark.parametrize("mode", ["exact", "fast_software", "fast"])
+def test_vs_reference_shader_golden(cuda, orc, renderer, gpu_textures, mode):
+    # compute-clouds.comp itself, compiled as C++ on the CPU (tests/golden/shader_clouds_1080p.npz):
+    # the exact kernel within 2e-4 relative on every pixel (it equals the FP32 restatement bit for
+    # bit, which the CPU tests hold to that bound); the production kernels within the FP64 gates.
+    import marshmallow as mm
+    import marshmallow.lib as L
+    import shader_golden as sg
+    opts = {"exact": dict(sampler=L.SAMPLER_SOFTWARE, math=L.MATH_EXACT), "fast_software": dict(sampler=L.SAMPLER_SOFTWARE),
+            "fast": {}}[mode]
+    night = mm.render.Textures.from_arrays({"night_sky": sg.night_sky(orc)})
+    handles = dict(gpu_textures.handles)
+    handles["night_sky"] = night.handles["night_sky"]
+    tex = mm.render.Textures(handles=handles)
+    for name, u, rows, cols, ref in sg.frames():
+        rgba, _ = render(cuda, renderer, u, tex, 1920, 1080, depth=False, pixel_mode=L.PIXELS_PHASE16, ref_uv_1080p=1,
+                         **opts)
+        got = rgba[rows][:, cols]
+        if mode == "exact":
+            assert sg.max_rel(got, ref) <= 2e-4, name
+        else:
+            e = mm.metrics.frame_errors(got, ref)
+            print(mode, name, e)
+            assert e["nan"] == 0 and e["rmse_255"] <= 1.0 and e["p999_255"] <= 4.0, (name, e)
+            assert e["frac_over_4"] <= 0.002, (name, e)
+    night.close()
+
+
 def test_coverage_offset_and_sun_sweep(cuda, orc, renderer, gpu_textures, host_textures):
     import marshmallow as mm
     import marshmallow.lib as L

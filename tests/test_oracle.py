@@ -250,3 +250,83 @@ def test_post_chain_night_skips_the_sun_passes(orc):
     u = mm.scene.uniforms(64, 48, sun_elevation=-10.0)
     img = np.random.default_rng(2).uniform(0, 3, (48, 64, 4)).astype(np.float32)
     assert np.array_equal(orc.post_chain(u, img), orc.post_tonemap(img))
+
+
+# ------------------------------------------------------------------------------------------------
+# The restatement against the reference shader itself: compute-clouds.comp compiled unchanged as
+# C++ on the CPU (oracle/Makefile `ref`, oracle/ref/glsl_to_cpp.py + glsl_shim.h).  Both evaluate
+# the same float expressions in the same order under the same sampler definition, so they agree to
+# the last few ulps of the elementary functions (libm's here, mm_math.h's in the restatement) and
+# take the same branch at every march threshold on these frames.
+
+def _shader_textures(orc, oracle_textures, u):
+    import shader_golden
+    return dict(oracle_textures, night_sky=shader_golden.night_sky(orc) if u.sun.direction[1] < 0 else None)
+
+
+def test_oracle_matches_reference_shader_golden(orc, oracle_textures):
+    import marshmallow as mm
+    import shader_golden as sg
+    frames = sg.frames()
+    assert len(frames) == 5
+    for name, u, rows, cols, ref in frames:
+        t = _shader_textures(orc, oracle_textures, u)
+        o32 = sg.oracle_march(orc, u, t, rows, cols, 32)
+        assert sg.max_rel(o32, ref) <= 2e-4, name
+        o64 = sg.oracle_march(orc, u, t, rows, cols, 64)
+        e = mm.metrics.frame_errors(o64, ref)
+        assert e["nan"] == 0 and e["rmse_255"] <= 1.0 and e["p999_255"] <= 4.0 and e["frac_over_4"] <= 0.002, (name, e)
+
+
+def test_reference_shader_build_reproduces_golden(orc, oracle_textures):
+    # Where the reference shader has been compiled (`make -C oracle ref`), it reproduces the fixture.
+    import shader_golden as sg
+    if not orc.ref_clouds_available():
+        pytest.skip("reference shader not compiled here")
+    for name, u, rows, cols, ref in sg.frames():
+        ys, xs = np.meshgrid(rows, cols, indexing="ij")
+        got = orc.ref_clouds_march(u, _shader_textures(orc, oracle_textures, u), xs.ravel(), ys.ravel())
+        assert sg.max_rel(got.reshape(ref.shape), ref) <= 1e-6, name
+
+
+def test_reference_shader_rejects_pixels_outside_the_phase(orc, oracle_textures):
+    import marshmallow as mm
+    if not orc.ref_clouds_available():
+        pytest.skip("reference shader not compiled here")
+    u = mm.scene.uniforms(1920, 1080, phase=6)
+    with pytest.raises(RuntimeError):
+        orc.ref_clouds_march(u, oracle_textures, np.array([2, 3]), np.array([1, 1]))
+    with pytest.raises(RuntimeError):
+        orc.ref_clouds_march(u, oracle_textures, np.array([1922]), np.array([1]))
+
+
+def test_oracle_matches_reference_shader_on_shipped_textures(orc, mmlib):
+    # The shipped Nubis textures (MM_ASSET_DIR = the reference's Textures/ folder), several poses.
+    import marshmallow as mm
+    import shader_golden as sg
+    from test_assets import _decode
+    root = os.environ.get("MM_ASSET_DIR")
+    if not root or not orc.ref_clouds_available():
+        pytest.skip("needs MM_ASSET_DIR and the compiled reference shader")
+
+    def image(name):
+        rc, a = _decode(mmlib, os.path.join(root, name))
+        assert rc == 0, name
+        return a
+
+    t = {"weather": image("CloudPlacement.png"), "night_sky": image("NightSky/nightSky_noOrange.png"),
+         "curl": image("CurlNoiseFBM.png"),
+         "low_res": np.stack([image("3DTextures/lowResCloudShape/lowResCloud(%d).tga" % i) for i in range(128)]),
+         "hi_res": np.stack([image("3DTextures/hiResCloudShape/hiResClouds (%d).tga" % i) for i in range(32)])}
+    poses = [dict(yaw=0.0, pitch=15.0, sun_elevation=30.0, phase=0),
+             dict(yaw=75.0, pitch=3.0, sun_elevation=8.0, time=120.0, phase=9),
+             dict(yaw=210.0, pitch=30.0, sun_elevation=55.0, time=600.0, phase=14),
+             dict(yaw=330.0, pitch=6.0, sun_elevation=-15.0, phase=7)]
+    for pose in poses:
+        u = mm.scene.uniforms(1920, 1080, **pose)
+        p = pose["phase"]
+        rows, cols = np.arange(p // 4, 1080, 16), np.arange(p % 4, 1920, 16)
+        ys, xs = np.meshgrid(rows, cols, indexing="ij")
+        ref = orc.ref_clouds_march(u, t, xs.ravel(), ys.ravel()).reshape(len(rows), len(cols), 4)
+        o32 = sg.oracle_march(orc, u, t, rows, cols, 32)
+        assert sg.max_rel(o32, ref) <= 2e-4, pose

@@ -358,8 +358,8 @@ int mm_mesh_shadow(mm_context ctx, const mm_uniforms* u, const mm_scene_textures
 /* ------------------------------------------------------------------------------------------ */
 /* Post chain: the reference's offscreen passes after the clouds (VulkanApplication.cpp:926-1010)  */
 /* as CUDA kernels on device buffers (no graphics API): god rays (god-ray.frag:41-76), radial      */
-/* blur (radialBlur.frag:112-139), the mesh over the blurred sky, Uncharted-2 tonemap + vignette  */
-/* (tonemap.frag:150-173) into the 8-bit swapchain layout.                                        */
+/* blur (radialBlur.frag:36-63), the mesh over the blurred sky, Uncharted-2 tonemap + vignette  */
+/* (tonemap.frag:11-33) into the 8-bit swapchain layout.                                        */
 /* ------------------------------------------------------------------------------------------ */
 
 typedef struct mm_post_options {

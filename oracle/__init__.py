@@ -161,6 +161,90 @@ def ref_clouds_march(uniforms, textures, xs, ys, nthreads=0):
     return out
 
 
+_ref_shaders = {}
+
+
+def _ref_shader(name):
+    """oracle/_ref/lib<name>.so: a reference shader compiled as C++ (`make -C oracle ref`), or None."""
+    path = os.path.join(ORACLE_DIR, "_ref", "lib%s.so" % name)
+    if name not in _ref_shaders:
+        _ref_shaders[name] = C.CDLL(path) if os.path.exists(path) else None
+    return _ref_shaders[name]
+
+
+def ref_reproject_available():
+    return _ref_shader("ref_reproject") is not None
+
+
+def ref_reproject(uniforms, src_rgba, nthreads=0):
+    """The reference's reproject.comp (compiled from its GLSL on the CPU) over a whole (h, w, 4) image."""
+    lib = _ref_shader("ref_reproject")
+    lib.ref_reproject.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int]
+    src = np.ascontiguousarray(src_rgba, np.float32)
+    h, w = src.shape[:2]
+    dst = np.zeros_like(src)
+    rc = lib.ref_reproject(C.addressof(uniforms), src.ctypes.data, w, h, dst.ctypes.data, nthreads)
+    if rc:
+        raise RuntimeError("ref_reproject failed: %d" % rc)
+    return dst
+
+
+def ref_post_available(which):
+    return _ref_shader("ref_" + which) is not None
+
+
+def ref_post(which, uniforms, src, nthreads=0):
+    """The reference's fragment shader (which = "god_ray" | "radial_blur" | "tonemap", compiled from its
+    GLSL on the CPU) shading every pixel of a full-screen pass over the (h, w, 4) float32 image src.
+    Returns outColor as (h, w, 4) float32 (the 8-bit conversion of the swapchain is left to the caller)."""
+    lib = _ref_shader("ref_" + which)
+    fn = getattr(lib, "ref_" + which)
+    fn.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int]
+    a = np.ascontiguousarray(src, np.float32)
+    out = np.zeros_like(a)
+    if fn(C.addressof(uniforms) if uniforms is not None else None, a.ctypes.data, a.shape[1], a.shape[0],
+          out.ctypes.data, nthreads):
+        raise RuntimeError("ref_%s failed" % which)
+    return out
+
+
+def ref_model_available():
+    return _ref_shader("ref_model") is not None
+
+
+def ref_model_shadow(uniforms, textures, world_pos, nthreads=0):
+    """The cloud shadow of the reference's model.frag (compiled from its GLSL on the CPU) at world
+    positions (n, 4): shades each fragment with and without clouds and returns accumDensity =
+    (1 - shadowed / clear) / 2 from the brightest channel, NaN where the shadowed colour is clamped to 0
+    (accumDensity >= 0.5; the shader keeps no more of it)."""
+    lib = _ref_shader("ref_model")
+    lib.ref_model_shade.argtypes = [C.c_void_p, C.POINTER(OracleTextures), C.c_void_p, C.c_size_t, C.c_void_p,
+                                    C.c_void_p, C.c_int]
+    keep, t = _textures(textures)
+    wp = np.ascontiguousarray(world_pos, np.float32).reshape(-1, 4)
+    n = wp.shape[0]
+    shadowed = np.zeros((n, 3), np.float32)
+    clear = np.zeros((n, 3), np.float32)
+    if lib.ref_model_shade(C.addressof(uniforms), C.byref(t), wp.ctypes.data, n, shadowed.ctypes.data,
+                           clear.ctypes.data, nthreads):
+        raise RuntimeError("ref_model_shade failed")
+    k = np.argmax(clear, axis=1)
+    c0 = clear[np.arange(n), k].astype(np.float64)
+    c = shadowed[np.arange(n), k].astype(np.float64)
+    if np.any(c0 <= 0):
+        raise RuntimeError("unlit fragment: the shadow cannot be recovered")
+    a = (1.0 - c / c0) * 0.5
+    a[c <= 0] = np.nan
+    return a
+
+
+def unorm8(x):
+    """Float -> UNORM8 as the swapchain stores a colour: clamp to [0, 1], scale by 255 in float, round to
+    nearest even."""
+    v = np.clip(np.nan_to_num(np.asarray(x, np.float32), nan=0.0), np.float32(0), np.float32(1))
+    return np.rint(v * np.float32(255)).astype(np.uint8)
+
+
 def shadow(uniforms, textures, world_pos, precision=32, coverage_offset=0.0, nthreads=0):
     """model.frag's cloud-shadow march over a G-buffer of world positions (..., 4) -> shadow (...)."""
     lib = load()

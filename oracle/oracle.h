@@ -86,7 +86,7 @@ int oracle_shadow_f32(const mm_uniforms* u, const oracle_textures* t, const floa
 int oracle_shadow_f64(const mm_uniforms* u, const oracle_textures* t, const float* world_pos, size_t n,
                       float coverage_offset, float* out_shadow, int nthreads);
 
-/* The post chain (god-ray.frag:41-76, radialBlur.frag:112-139, tonemap.frag:150-173) on w x h RGBA32F
+/* The post chain (god-ray.frag:41-76, radialBlur.frag:36-63, tonemap.frag:11-33) on w x h RGBA32F
  * images (rows of 4 floats).  god_rays: dst = (src.rgb, god-ray term); radial_blur: dst =
  * (sun colour * intensity * blur(src.a) + 0.5 src.rgb, 1); tonemap: 8-bit (bgra: B,G,R,A byte order
  * as the B8G8R8A8 swapchain, else R,G,B,A; A = 255).  chain: clouds -> god rays -> radial blur ->

@@ -1,7 +1,7 @@
 // oracle_post.cpp - CPU restatement of the reference's post-processing chain (test infrastructure
 // only): god rays (SkyEngine/SkyEngine/Shaders/god-ray.frag:41-76), radial blur
-// (radialBlur.frag:112-139), the mesh drawn over the blurred sky in the same render pass
-// (VulkanApplication.cpp:955-966) and the Uncharted-2 tonemap with vignette (tonemap.frag:150-173)
+// (radialBlur.frag:36-63), the mesh drawn over the blurred sky in the same render pass
+// (VulkanApplication.cpp:955-966) and the Uncharted-2 tonemap with vignette (tonemap.frag:11-33)
 // into the 8-bit swapchain image (B8G8R8A8_UNORM, VulkanApplication.cpp:1437-1446).
 //
 // Conventions shared with the CUDA kernels (post.cu):
@@ -12,8 +12,9 @@
 //    LINEAR filter's weights are zero there); taps elsewhere are bilinear with float weights and
 //    CLAMP_TO_EDGE (the offscreen sampler, VulkanApplication.cpp:1290-1305): x = u W - 0.5,
 //    a = x - floor(x), indices clamped to the image;
-//  - camera.proj * camera.view * sun.location is evaluated as (proj * view) * location, sums in
-//    index order;
+//  - camera.proj * camera.view * sun.location is evaluated as (proj * view) * location, the
+//    elements of the matrix product summed in index order, the matrix-vector product pairwise
+//    (glm's orders, under which the compiled shaders agree with this file);
 //  - GLSL constant expressions (SAMPLE_WEIGHT * DENSITY, the tonemap's 0.1 * 0.5 ...) are folded in
 //    float; pow is mm_math.h's powf; the float -> UNORM8 conversion rounds to nearest even after
 //    clamping to [0, 1] (NaN -> 0).
@@ -59,7 +60,9 @@ float sample_channel(const Img& im, float u, float v, int c) {
     return mixf(a, b, ay);
 }
 
-// (proj * view) * sun.location, divided by its w (god-ray.frag:44-46, radialBlur.frag:124-125).
+// (proj * view) * sun.location, divided by its w (god-ray.frag:44-46, radialBlur.frag:48-49).
+// GLSL leaves the order of the sums to its compiler; these are glm's: each element of the matrix
+// product summed in index order, the matrix-vector product pairwise, (m0 x + m1 y) + (m2 z + m3 w).
 void sun_ndc(const mm_uniforms* u, float* sx, float* sy) {
     const float* P = u->camera.proj;
     const float* V = u->camera.view;
@@ -72,7 +75,7 @@ void sun_ndc(const mm_uniforms* u, float* sx, float* sy) {
         }
     const float* L = u->sun.location;
     float q[4];
-    for (int r = 0; r < 4; ++r) q[r] = ((pv[0 * 4 + r] * L[0] + pv[1 * 4 + r] * L[1]) + pv[2 * 4 + r] * L[2]) + pv[3 * 4 + r] * L[3];
+    for (int r = 0; r < 4; ++r) q[r] = (pv[0 * 4 + r] * L[0] + pv[1 * 4 + r] * L[1]) + (pv[2 * 4 + r] * L[2] + pv[3 * 4 + r] * L[3]);
     *sx = q[0] / q[3];
     *sy = q[1] / q[3];
 }
@@ -117,7 +120,7 @@ void god_rays(const mm_uniforms* un, const Img& src, float* dst) {
         }
 }
 
-// radialBlur.frag:112-139
+// radialBlur.frag:36-63
 void radial_blur(const mm_uniforms* un, const Img& src, float* dst) {
     static const float kTaps[10] = {-0.08f, -0.05f, -0.03f, -0.02f, -0.01f, 0.01f, 0.02f, 0.03f, 0.05f, 0.08f};
     float sx, sy;
@@ -155,7 +158,7 @@ void radial_blur(const mm_uniforms* un, const Img& src, float* dst) {
         }
 }
 
-// tonemap.frag:150-153
+// tonemap.frag:11-14
 inline float uc2(float x) {
     return ((x * (0.15f * x + 0.1f * 0.5f) + 0.2f * 0.02f) / (x * (0.15f * x + 0.5f) + 0.2f * 0.3f)) - 0.02f / 0.3f;
 }
@@ -165,7 +168,7 @@ inline uint8_t unorm8(float v) {
     return (uint8_t)nearbyintf(v * 255.0f);
 }
 
-// tonemap.frag:155-173 into 8 bits
+// tonemap.frag:16-33 into 8 bits
 void tonemap(const Img& src, uint8_t* out, size_t pitch, int bgra) {
     const float whitemap = 1.0f / uc2(50.2f);
     const float inv_gamma = 1.0f / 2.2f;

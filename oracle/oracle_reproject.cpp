@@ -56,10 +56,12 @@ extern "C" int oracle_reproject_f32(const mm_uniforms* u, const float* src_rgba,
             v3 p = sub(add(ref, mul(cpx * sx * cpy, right)), mul(sy * cpy, up));
             const v3 rd = normalize(sub(p, cam));
             v3 ip = sphere_point(cam, rd, center, 2000000.0f);  // :120
-            // (cameraPrev.view * vec4(ip, 1)).xyz (:125)
-            v3 q = {((pv[0] * ip.x + pv[4] * ip.y) + pv[8] * ip.z) + pv[12],
-                    ((pv[1] * ip.x + pv[5] * ip.y) + pv[9] * ip.z) + pv[13],
-                    ((pv[2] * ip.x + pv[6] * ip.y) + pv[10] * ip.z) + pv[14]};
+            // (cameraPrev.view * vec4(ip, 1)).xyz (:125).  GLSL leaves the order of the sum to its
+            // compiler; this is glm's, (m0 x + m1 y) + (m2 z + m3 w), so the restatement equals the
+            // shader compiled on glm bit for bit.
+            v3 q = {(pv[0] * ip.x + pv[4] * ip.y) + (pv[8] * ip.z + pv[12]),
+                    (pv[1] * ip.x + pv[5] * ip.y) + (pv[9] * ip.z + pv[13]),
+                    (pv[2] * ip.x + pv[6] * ip.y) + (pv[10] * ip.z + pv[14])};
             v3 od = normalize(q);
             const float nz = -od.z;
             od = {od.x / nz, od.y / nz, od.z / nz};  // :132

@@ -11,7 +11,8 @@
 //    host thread at a time); `in`/`inout` parameter qualifiers vanish (the shaders read their
 //    inout parameters back nowhere);
 //  - vec/mat types and the built-in functions are glm's (swizzles included), with float overloads
-//    for the calls GLSL makes with integer literals (clamp(x, 0, 1) and the like);
+//    for the calls GLSL makes with integer literals (clamp(x, 0, 1) and the like) and the implicit
+//    int -> float conversion of mixed vector arithmetic;
 //  - samplers: LINEAR filter with float weights, REPEAT or CLAMP_TO_EDGE, mip 0, on UNORM8 or float
 //    texels — the definition shared with the CPU restatement (x = u*N - 0.5, i0 = floor(x),
 //    a = x - i0, interpolated along x, then y, then z);
@@ -46,6 +47,18 @@ inline float min(float a, float b) { return glm::min(a, b); }
 inline float max(float a, float b) { return glm::max(a, b); }
 inline float mix(float a, float b, float t) { return glm::mix(a, b, t); }
 inline float smoothstep(float e0, float e1, float x) { return glm::smoothstep(e0, e1, x); }
+
+// GLSL converts an integer vector operand to float implicitly (vec2(uv) / ivec2(dim)); glm does not.
+template <length_t L>
+inline vec<L, float> operator*(const vec<L, float>& a, const vec<L, int>& b) { return a * vec<L, float>(b); }
+template <length_t L>
+inline vec<L, float> operator*(const vec<L, int>& a, const vec<L, float>& b) { return vec<L, float>(a) * b; }
+template <length_t L>
+inline vec<L, float> operator/(const vec<L, float>& a, const vec<L, int>& b) { return a / vec<L, float>(b); }
+template <length_t L>
+inline vec<L, float> operator+(const vec<L, float>& a, const vec<L, int>& b) { return a + vec<L, float>(b); }
+template <length_t L>
+inline vec<L, float> operator-(const vec<L, float>& a, const vec<L, int>& b) { return a - vec<L, float>(b); }
 
 // ---------------------------------------------------------------------------------- samplers
 

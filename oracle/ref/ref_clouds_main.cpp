@@ -12,29 +12,10 @@
 #include <thread>
 #include <vector>
 
-#include "../oracle.h"
-
 #include "compute_clouds.gen.cpp"
-// the shim's GLSL keywords end with the shader
-#undef main
-#undef layout
-#undef uniform
-#undef readonly
-#undef writeonly
-#undef highp
-#undef in
-#undef inout
-#undef out
+#include "ref_uniforms.h"
 
 namespace {
-
-mat4 to_mat4(const float* m) {  // std140 column-major, as glm stores it
-    mat4 r;
-    std::memcpy(&r[0][0], m, 16 * sizeof(float));
-    return r;
-}
-
-vec4 to_vec4(const float* v) { return vec4(v[0], v[1], v[2], v[3]); }
 
 void bind(GlslSampler& s, const oracle_texture& t) {
     s.texels = t.texels;
@@ -60,22 +41,7 @@ int ref_clouds_march(const mm_uniforms* u, const oracle_textures* t, const int* 
         if (xs[i] < 0 || ys[i] < 0 || xs[i] >= WIDTH || ys[i] >= HEIGHT) return -1;
         if (xs[i] % 4 != phase % 4 || ys[i] % 4 != phase / 4) return -1;
     }
-    camera.view = to_mat4(u->camera.view);
-    camera.proj = to_mat4(u->camera.proj);
-    camera.cameraPosition = to_vec4(u->camera.camera_position);
-    camera.cameraParams = to_vec4(u->camera.camera_params);
-    cameraPrev.view = to_mat4(u->camera_prev.view);
-    cameraPrev.proj = to_mat4(u->camera_prev.proj);
-    cameraPrev.cameraPosition = to_vec4(u->camera_prev.camera_position);
-    sun.location = to_vec4(u->sun.location);
-    sun.direction = to_vec4(u->sun.direction);
-    sun.color = to_vec4(u->sun.color);
-    sun.directionBasis = to_mat4(u->sun.direction_basis);
-    sun.intensity = u->sun.intensity;
-    sky.betaR = to_vec4(u->sky.beta_r);
-    sky.betaV = to_vec4(u->sky.beta_v);
-    sky.wind = to_vec4(u->sky.wind);
-    sky.mie_directional = u->sky.mie_directional;
+    refshader::load_blocks(u, camera, cameraPrev, sun, sky);
     bind(cloudPlacement, t->weather);
     bind(nightSkyMap, t->night_sky);
     bind(curlNoise, t->curl);
@@ -87,19 +53,10 @@ int ref_clouds_march(const mm_uniforms* u, const oracle_textures* t, const int* 
     resultImage.w = WIDTH;
     resultImage.h = HEIGHT;
 
-    if (nthreads <= 0) nthreads = (int)std::thread::hardware_concurrency();
-    if (nthreads <= 0) nthreads = 1;
-    std::atomic<size_t> next{0};
-    auto work = [&]() {
-        for (size_t i; (i = next.fetch_add(1)) < n;) {
-            gl_GlobalInvocationID = uvec3((unsigned)xs[i] / 4u, (unsigned)ys[i] / 4u, 0u);
-            glsl_main();
-        }
-    };
-    std::vector<std::thread> pool;
-    for (int k = 1; k < nthreads; ++k) pool.emplace_back(work);
-    work();
-    for (auto& th : pool) th.join();
+    refshader::parallel_for(n, nthreads, [&](size_t i) {
+        gl_GlobalInvocationID = uvec3((unsigned)xs[i] / 4u, (unsigned)ys[i] / 4u, 0u);
+        glsl_main();
+    });
 
     for (size_t i = 0; i < n; ++i)
         std::memcpy(out + 4 * i, &image[((size_t)ys[i] * WIDTH + xs[i]) * 4], 4 * sizeof(float));

@@ -12,12 +12,13 @@ int launch_post_exact(const PostLaunch& p, int which, cudaStream_t s);
 
 namespace {
 
-float uc2_host(float x) {  // tonemap.frag:150-153, host twin of post::uc2
+float uc2_host(float x) {  // tonemap.frag:11-14, host twin of post::uc2
     return ((x * (0.15f * x + 0.1f * 0.5f) + 0.2f * 0.02f) / (x * (0.15f * x + 0.5f) + 0.2f * 0.3f)) - 0.02f / 0.3f;
 }
 
-// (proj * view) * sun.location / w (god-ray.frag:44-46): the product of the matrices first, sums in
-// index order, as the CPU restatement evaluates it.
+// (proj * view) * sun.location / w (god-ray.frag:44-46): the product of the matrices first (each
+// element summed in index order), then the matrix-vector product summed pairwise,
+// (m0 x + m1 y) + (m2 z + m3 w), as the CPU restatement evaluates both.
 void sun_ndc(const mm_uniforms& u, float* sx, float* sy) {
     const float* P = u.camera.proj;
     const float* V = u.camera.view;
@@ -30,7 +31,7 @@ void sun_ndc(const mm_uniforms& u, float* sx, float* sy) {
         }
     const float* L = u.sun.location;
     float q[4];
-    for (int r = 0; r < 4; ++r) q[r] = ((pv[r] * L[0] + pv[4 + r] * L[1]) + pv[8 + r] * L[2]) + pv[12 + r] * L[3];
+    for (int r = 0; r < 4; ++r) q[r] = (pv[r] * L[0] + pv[4 + r] * L[1]) + (pv[8 + r] * L[2] + pv[12 + r] * L[3]);
     *sx = q[0] / q[3];
     *sy = q[1] / q[3];
 }

@@ -1,7 +1,7 @@
 // post_kernel.cuh - the reference's post-processing chain as CUDA kernels, headless: god rays
-// (god-ray.frag:41-76), radial blur (radialBlur.frag:112-139), the mesh drawn over the blurred
+// (god-ray.frag:41-76), radial blur (radialBlur.frag:36-63), the mesh drawn over the blurred
 // sky (VulkanApplication.cpp:955-966) and the Uncharted-2 tonemap with vignette
-// (tonemap.frag:150-173) into an 8-bit image laid out as the B8G8R8A8 swapchain (or R8G8B8A8).
+// (tonemap.frag:11-33) into an 8-bit image laid out as the B8G8R8A8 swapchain (or R8G8B8A8).
 //
 // The reference runs each pass as a full-screen quad into an RGBA32F framebuffer.  The chain here
 // is two kernels: the god-ray term (the only value of the god-ray framebuffer that is not a copy
@@ -117,7 +117,7 @@ __device__ __forceinline__ float god_ray_term(const PostLaunch& p, const Taps& a
     return accum * 0.9f;
 }
 
-// radialBlur.frag:127-136: the mean of ten taps of the god-ray term along the line to the sun.
+// radialBlur.frag:51-60: the mean of ten taps of the god-ray term along the line to the sun.
 template <class Taps>
 __device__ __forceinline__ float radial_term(const PostLaunch& p, const Taps& g, float px, float py) {
     float lx = p.sun_x - px, ly = p.sun_y - py;
@@ -134,7 +134,7 @@ __device__ __forceinline__ float radial_term(const PostLaunch& p, const Taps& g,
     return accum / 10.0f;
 }
 
-__device__ __forceinline__ float uc2(float x) {  // tonemap.frag:150-153
+__device__ __forceinline__ float uc2(float x) {  // tonemap.frag:11-14
     return ((x * (0.15f * x + 0.1f * 0.5f) + 0.2f * 0.02f) / (x * (0.15f * x + 0.5f) + 0.2f * 0.3f)) - 0.02f / 0.3f;
 }
 
@@ -146,7 +146,7 @@ __device__ __forceinline__ float powf_(float x, float y) {
 
 __device__ __forceinline__ uint32_t unorm8(float v) { return (uint32_t)__float2int_rn(fminf(fmaxf(v, 0.0f), 1.0f) * 255.0f); }
 
-// tonemap.frag:163-172 for colour c at uv (u, v); packed 8-bit texel.
+// tonemap.frag:24-33 for colour c at uv (u, v); packed 8-bit texel.
 template <bool E>
 __device__ __forceinline__ uint32_t tonemap8(const PostLaunch& p, float r, float g, float b, float u, float v) {
     const float inv_gamma = 1.0f / 2.2f;

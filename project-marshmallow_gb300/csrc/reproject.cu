@@ -74,9 +74,10 @@ __global__ void __launch_bounds__(256) reproject_kernel(P p) {
     const v3 q0 = sub(add(ref, mul(cpx * sx * cpy, right)), mul(sy * cpy, up));
     const v3 rd = normalize(sub(q0, cam));
     const v3 ip = sphere_point(cam, rd, center, 2000000.0f);
-    const v3 q = {((pv[0] * ip.x + pv[4] * ip.y) + pv[8] * ip.z) + pv[12],
-                  ((pv[1] * ip.x + pv[5] * ip.y) + pv[9] * ip.z) + pv[13],
-                  ((pv[2] * ip.x + pv[6] * ip.y) + pv[10] * ip.z) + pv[14]};
+    // (cameraPrev.view * vec4(ip, 1)).xyz, summed pairwise as the CPU restatement does
+    const v3 q = {(pv[0] * ip.x + pv[4] * ip.y) + (pv[8] * ip.z + pv[12]),
+                  (pv[1] * ip.x + pv[5] * ip.y) + (pv[9] * ip.z + pv[13]),
+                  (pv[2] * ip.x + pv[6] * ip.y) + (pv[10] * ip.z + pv[14])};
     v3 od = normalize(q);
     const float nz = -od.z;
     od = {__fdiv_rn(od.x, nz), __fdiv_rn(od.y, nz), __fdiv_rn(od.z, nz)};

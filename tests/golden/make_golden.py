@@ -17,6 +17,11 @@
                       seed-0 generator textures: for five frames (sweep poses, a low sun, a night sky;
                       pixel phases 0, 5, 10, 15, 3) the rgba of every 32nd pixel of the phase in x and y
                       of its hard-coded 1920x1080 frame, with the uniform blocks that made them.
+  shader_passes.npz   the reference's reproject.comp, model.frag, god-ray.frag, radialBlur.frag and
+                      tonemap.frag compiled the same way: SHA-256 of the reprojected images of three
+                      camera motions (tests/shader_golden.py REPROJECT_CASES, seeded hash images);
+                      the god-ray alpha, radial-blur rgb and tonemap rgb (8 bits) of a 64x36 frame;
+                      the cloud shadow of a 48x27 terrain G-buffer (positions stored with it).
   asset_digests.json  SHA-256 of the RGBA8 decode (stbi_load(..., STBI_rgb_alpha) conventions) of the
                       shipped textures the reference loads, from the independent decoders in
                       tests/tga.py and tests/png.py; the library's loader must reproduce them.
@@ -125,6 +130,48 @@ def shader_clouds_golden():
                         uniforms=np.stack(ublocks), rgba=np.stack(images), stride=SHADER_STRIDE)
 
 
+def shader_passes_golden():
+    import ctypes as C
+    sys.path.insert(0, os.path.join(REPO, "project-marshmallow_gb300"))
+    sys.path.insert(0, REPO)
+    import oracle
+    import marshmallow as mm
+    import marshmallow.lib as L
+    import shader_golden as sg
+
+    def ublock(u):
+        return np.frombuffer(C.string_at(C.addressof(u), C.sizeof(u)), np.uint8)
+
+    out = {}
+    digests, ubs = [], []
+    for k, case in enumerate(sg.REPROJECT_CASES):
+        u = sg.reproject_uniforms(case)
+        src = sg.pattern(case[1], case[0], k)
+        digests.append(sg.digest(oracle.ref_reproject(u, src)))
+        ubs.append(ublock(u))
+    out["reproject_uniforms"] = np.stack(ubs)
+    out["reproject_digests"] = np.array(digests)
+
+    u = sg.post_uniforms()
+    w, h = sg.POST_SIZE
+    src = sg.pattern(h, w, 11)
+    g = oracle.ref_post("god_ray", u, src)
+    out["post_uniforms"] = ublock(u)
+    out["god_ray_alpha"] = g[..., 3]
+    out["radial_blur_rgb"] = oracle.ref_post("radial_blur", u, g)[..., :3]
+    out["tonemap_rgb"] = oracle.unorm8(oracle.ref_post("tonemap", None, src)[..., :3])
+
+    w, h = sg.SHADOW_SIZE
+    u = mm.scene.uniforms(w, h, eye=(0.0, 150.0, 0.0), pitch=-20.0, sun_elevation=35.0, time=20.0)
+    gb = mm.scene.terrain_gbuffer(u, w, h).astype(np.float32)
+    tex = {"low_res": oracle.noise(L.NOISE_LOWRES, 0, 128, 128, 128, 4),
+           "weather": oracle.noise(L.NOISE_WEATHER, 0, 512, 512, 1, 4)[0]}
+    out["shadow_uniforms"] = ublock(u)
+    out["shadow_world_pos"] = gb
+    out["shadow"] = oracle.ref_model_shadow(u, tex, gb.reshape(-1, 4)).reshape(h, w).astype(np.float32)
+    np.savez_compressed(os.path.join(HERE, "shader_passes.npz"), **out)
+
+
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     ref = args[0] if args else "/root/reference"
@@ -135,6 +182,7 @@ def main():
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", "REF=" + ref], check=True)
     bins = os.path.join(REPO, "oracle", "_ref")
     shader_clouds_golden()
+    shader_passes_golden()
     if "--shader-only" in sys.argv:
         return
 

@@ -43,3 +43,54 @@ def max_rel(a, ref, floor=1e-3):
     a = np.asarray(a, np.float64)
     ref = np.asarray(ref, np.float64)
     return float((np.abs(a - ref) / np.maximum(np.abs(ref), floor)).max())
+
+
+# ------------------------------------------------------------------------------------------------
+# The other passes: reproject.comp, model.frag's cloud shadow, god-ray.frag, radialBlur.frag and
+# tonemap.frag, compiled the same way (tests/golden/shader_passes.npz).
+
+PASSES = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "shader_passes.npz")
+
+# (width, height, yaw step, pitch step, eye offset) of the reprojection cases: the previous frame looks
+# from yaw 20, pitch 10 at (0, 10, 0); the current one turns by the steps and moves by the offset.
+REPROJECT_CASES = [(1920, 1080, 0.7, -0.4, (0.0, 50.0, 30.0)), (320, 180, -5.0, 2.0, (0.0, 50.0, 30.0)),
+                   (333, 127, 10.0, 5.0, (0.0, 0.0, 0.0))]
+POST_SIZE = (64, 36)
+SHADOW_SIZE = (48, 27)
+
+
+def pattern(h, w, seed, rgb_scale=20.0):
+    """A seeded (h, w, 4) float32 image from an integer hash (the same bits on every machine): rgb in
+    [0, rgb_scale), alpha in [0, 1)."""
+    i = np.arange(h * w * 4, dtype=np.uint64).reshape(h, w, 4)
+    x = (i * np.uint64(2654435761) + np.uint64(seed) * np.uint64(40503)) & np.uint64(0xFFFFFFFF)
+    x ^= x >> np.uint64(15)
+    x = (x * np.uint64(2246822519)) & np.uint64(0xFFFFFFFF)
+    x ^= x >> np.uint64(13)
+    v = (x >> np.uint64(8)).astype(np.float32) * np.float32(1.0 / (1 << 24))
+    return v * np.array([rgb_scale, rgb_scale, rgb_scale, 1.0], np.float32)
+
+
+def reproject_uniforms(case):
+    import ctypes as C
+    import marshmallow as mm
+    w, h, dyaw, dpitch, move = case
+    prev = mm.scene.uniforms(w, h, yaw=20.0, pitch=10.0)
+    cur = mm.scene.uniforms(w, h, eye=(move[0], 10.0 + move[1], move[2]), yaw=20.0 + dyaw, pitch=10.0 + dpitch)
+    C.memmove(C.addressof(cur.camera_prev), C.addressof(prev.camera), C.sizeof(cur.camera_prev))
+    return cur
+
+
+def post_uniforms():
+    import marshmallow as mm
+    return mm.scene.uniforms(POST_SIZE[0], POST_SIZE[1], yaw=0.0, pitch=12.0, sun_elevation=20.0)
+
+
+def digest(a):
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def passes():
+    z = np.load(PASSES)
+    return {k: z[k] for k in z.files}

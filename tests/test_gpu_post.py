@@ -133,3 +133,33 @@ def test_post_argument_errors(cuda, env):
     bad = L.PostOptions(7, 1)
     assert lib.mm_post_chain(r.ctx, C.byref(u), C.byref(img), None, out.data_ptr(), W * 4, C.byref(bad), None) == \
         L.MM_ERR_INVALID_ARGUMENT
+
+
+def test_exact_passes_vs_reference_shader_golden(cuda, env):
+    # god-ray.frag, radialBlur.frag and tonemap.frag themselves, compiled as C++ on the CPU
+    # (tests/golden/shader_passes.npz).  The exact kernels equal the CPU restatement, which differs
+    # from the compiled shaders only in the centre fetch (the texel itself here; a float-weight filter
+    # ~1e-5 of a texel off the centre there): within 3e-5 of each channel's largest input value, and
+    # the 8-bit tonemap within one step on at most 0.1% of the bytes.
+    import marshmallow.lib as L
+    import shader_golden as sg
+    _, r = env
+    z = sg.passes()
+    u = L.Uniforms.from_buffer_copy(z["post_uniforms"].tobytes())
+    w, h = sg.POST_SIZE
+    src_np = sg.pattern(h, w, 11)
+    src = cuda.from_numpy(src_np).cuda()
+    g = cuda.full_like(src, -1.0)
+    r.god_rays(u, src, g, math=L.MATH_EXACT)
+    b = cuda.full_like(src, -1.0)
+    r.radial_blur(u, g, b, math=L.MATH_EXACT)
+    out8 = cuda.zeros((h, w, 4), dtype=cuda.uint8, device="cuda")
+    r.tonemap(src, out8, math=L.MATH_EXACT)
+    cuda.cuda.synchronize()
+    g_np, b_np, t_np = g.cpu().numpy(), b.cpu().numpy(), out8.cpu().numpy()
+    bound_a = 3e-5 * np.abs(src_np[..., 3]).max() + 1e-7
+    assert np.abs(g_np[..., 3] - z["god_ray_alpha"]).max() <= bound_a
+    bound_rgb = 1.5e-5 * np.abs(g_np[..., :3]).reshape(-1, 3).max(0) + 1e-7
+    assert np.all(np.abs(b_np[..., :3] - z["radial_blur_rgb"]) <= bound_rgb)
+    d = np.abs(t_np[..., :3].astype(int) - z["tonemap_rgb"].astype(int))
+    assert d.max() <= 1 and (d > 0).mean() <= 1e-3

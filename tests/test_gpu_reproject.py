@@ -116,3 +116,21 @@ def test_frame_equals_sequential_passes(cuda, env, math):
         r.march(u, tex, b[0], b[1], pixel_mode=1, math=math)
         cuda.cuda.synchronize()
         assert cuda.equal(a[0], b[0]) and cuda.equal(a[1], b[1]), (k, phase)
+
+
+@pytest.mark.parametrize("k", range(3))
+def test_reproject_exact_equals_reference_shader_golden(cuda, env, k):
+    # reproject.comp itself, compiled as C++ on the CPU (tests/golden/shader_passes.npz): the exact
+    # kernel reproduces its image bit for bit (SHA-256 of the rgba).
+    import marshmallow.lib as L
+    import shader_golden as sg
+    _, r = env
+    z = sg.passes()
+    w, h = sg.REPROJECT_CASES[k][:2]
+    u = L.Uniforms.from_buffer_copy(z["reproject_uniforms"][k].tobytes())
+    src = cuda.from_numpy(sg.pattern(h, w, k)).cuda()
+    dst = cuda.full_like(src, -1.0)
+    sd, dd = cuda.zeros((h, w), device="cuda"), cuda.zeros((h, w), device="cuda")
+    r.reproject(u, (src, sd), (dst, dd), math=L.MATH_EXACT)
+    cuda.cuda.synchronize()
+    assert sg.digest(dst.cpu().numpy()) == str(z["reproject_digests"][k])

@@ -118,3 +118,26 @@ def test_device_gbuffer_matches_host_gbuffer(cuda, mmlib):
     b = mm.scene.terrain_gbuffer_cuda(u, 160, 90).cpu().numpy()
     assert np.array_equal(a[..., 3], b[..., 3])
     assert np.max(np.abs(a - b)) < 1e-2
+
+
+@pytest.mark.parametrize("mode", ["exact", "fast_hardware"])
+def test_shadow_vs_reference_shader_golden(cuda, env, mode):
+    # model.frag itself, compiled as C++ on the CPU, with the shadow recovered from its shaded colour
+    # (tests/golden/shader_passes.npz; NaN where the shadow is >= 0.5 and the colour clamps to 0).
+    import marshmallow.lib as L
+    import shader_golden as sg
+    tex, r = env
+    z = sg.passes()
+    u = L.Uniforms.from_buffer_copy(z["shadow_uniforms"].tobytes())
+    g = np.ascontiguousarray(z["shadow_world_pos"])
+    opts = dict(math=L.MATH_EXACT, sampler=L.SAMPLER_SOFTWARE) if mode == "exact" else dict(math=L.MATH_FAST,
+                                                                                         sampler=L.SAMPLER_HARDWARE)
+    got = _gpu_shadow(cuda, r, tex, u, g, **opts)
+    want = z["shadow"]
+    fin = np.isfinite(want)
+    err = np.abs(got[fin].astype(np.float64) - want[fin])
+    if mode == "exact":
+        assert err.max() <= 1e-6
+        assert np.all(got[~fin] >= 0.5 - 1e-6)
+    else:
+        assert err.mean() <= 2e-3 and (err > 0.01).mean() <= 5e-3

@@ -215,7 +215,7 @@ def test_shadow_saturates_and_vanishes(orc):
 
 def test_post_chain_known_answers(orc):
     # Uniform alpha a: each god-ray tap reads a, so the term is 0.9 * 0.5 a (1 + 0.125 sum 0.99^i)
-    # (god-ray.frag:56-75); the radial blur of a uniform term t is 1.1 t (radialBlur.frag:133-136).
+    # (god-ray.frag:56-75); the radial blur of a uniform term t is 1.1 t (radialBlur.frag:57-60).
     import marshmallow as mm
     u = mm.scene.uniforms(96, 64, yaw=0.0, pitch=15.0, sun_elevation=20.0)
     img = np.zeros((64, 96, 4), np.float32)
@@ -245,7 +245,7 @@ def test_post_chain_known_answers(orc):
 
 
 def test_post_chain_night_skips_the_sun_passes(orc):
-    # Sun below the horizon: both passes copy the colour (god-ray.frag:52-54, radialBlur.frag:117-119).
+    # Sun below the horizon: both passes copy the colour (god-ray.frag:52-54, radialBlur.frag:41-43).
     import marshmallow as mm
     u = mm.scene.uniforms(64, 48, sun_elevation=-10.0)
     img = np.random.default_rng(2).uniform(0, 3, (48, 64, 4)).astype(np.float32)
@@ -330,3 +330,122 @@ def test_oracle_matches_reference_shader_on_shipped_textures(orc, mmlib):
         ref = orc.ref_clouds_march(u, t, xs.ravel(), ys.ravel()).reshape(len(rows), len(cols), 4)
         o32 = sg.oracle_march(orc, u, t, rows, cols, 32)
         assert sg.max_rel(o32, ref) <= 2e-4, pose
+
+
+# The other passes against their shaders compiled the same way.  Reprojection is bit-identical (the
+# restatement sums cameraPrev.view * p in glm's pairwise order, one of the orders GLSL allows).  The
+# post passes differ only where the shader samples texColor at its own fragUV: the restatement takes
+# the texel (the filter's weights are zero at a texel centre on the GPU's fixed-point filter), the
+# shim's float-weight sampler lands ~1e-5 of a texel off the centre and mixes in that much of the
+# neighbour.  The shadow is recovered from the shaded colour (see oracle.ref_model_shadow).
+
+def _post_bound(src, channels):
+    """Error bound of the centre fetch: 3e-5 of the largest input value of each channel."""
+    return 3e-5 * np.abs(src[..., channels]).reshape(-1, len(channels)).max(0) + 1e-7
+
+
+def test_reprojection_matches_reference_shader_golden(orc):
+    import shader_golden as sg
+    import marshmallow.lib as L
+    z = sg.passes()
+    for k, (case, ub, want) in enumerate(zip(sg.REPROJECT_CASES, z["reproject_uniforms"], z["reproject_digests"])):
+        u = L.Uniforms.from_buffer_copy(ub.tobytes())
+        got, _ = orc.reproject(u, sg.pattern(case[1], case[0], k))
+        assert sg.digest(got) == str(want), case
+
+
+def test_post_passes_match_reference_shader_golden(orc):
+    import shader_golden as sg
+    import marshmallow.lib as L
+    z = sg.passes()
+    u = L.Uniforms.from_buffer_copy(z["post_uniforms"].tobytes())
+    w, h = sg.POST_SIZE
+    src = sg.pattern(h, w, 11)
+    g = orc.post_pass("god_rays", u, src)
+    assert np.array_equal(g[..., :3], src[..., :3])
+    assert np.all(np.abs(g[..., 3] - z["god_ray_alpha"]) <= _post_bound(src, [3]))
+    assert z["god_ray_alpha"].max() > 0.3  # the sun is in view
+    b = orc.post_pass("radial_blur", u, g)
+    assert np.all(np.abs(b[..., :3] - z["radial_blur_rgb"]) <= 0.5 * _post_bound(g, [0, 1, 2]))
+    t = orc.post_tonemap(src)[..., :3].astype(int)
+    d = np.abs(t - z["tonemap_rgb"].astype(int))
+    assert d.max() <= 1 and (d > 0).mean() <= 1e-3
+
+
+def test_shadow_matches_reference_shader_golden(orc, oracle_textures):
+    import shader_golden as sg
+    import marshmallow.lib as L
+    z = sg.passes()
+    u = L.Uniforms.from_buffer_copy(z["shadow_uniforms"].tobytes())
+    got = orc.shadow(u, oracle_textures, z["shadow_world_pos"])
+    want = z["shadow"]
+    fin = np.isfinite(want)
+    assert (want[fin] > 0).mean() > 0.2  # the G-buffer has cloud shadow to check
+    assert np.abs(got[fin] - want[fin]).max() <= 1e-6
+    assert np.all(got[~fin] >= 0.5 - 1e-6)
+
+
+def _need(available):
+    if not available:
+        pytest.skip("reference shader not compiled here")
+
+
+@pytest.mark.parametrize("k", range(3))
+def test_reprojection_equals_reference_shader_build(orc, k):
+    import shader_golden as sg
+    import marshmallow as mm
+    _need(orc.ref_reproject_available())
+    case = sg.REPROJECT_CASES[k]
+    u = sg.reproject_uniforms(case)
+    src = sg.pattern(case[1], case[0], k)
+    want = orc.ref_reproject(u, src)
+    got, _ = orc.reproject(u, src)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    # and a sweep of camera motions between consecutive frames
+    for frame in (1, 6, 13):
+        cur = mm.scene.sweep_uniforms(frame, 400, 224)
+        prev = mm.scene.sweep_uniforms(frame - 1, 400, 224)
+        cur.camera_prev = prev.camera_prev  # the previous frame's camera (set with it)
+        src = sg.pattern(224, 400, 100 + frame)
+        assert np.array_equal(orc.reproject(cur, src)[0], orc.ref_reproject(cur, src)), frame
+
+
+@pytest.mark.parametrize("elev,yaw", [(20.0, 0.0), (8.0, 25.0), (45.0, -30.0), (-6.0, 0.0)])
+def test_post_passes_match_reference_shader_build(orc, elev, yaw):
+    import shader_golden as sg
+    import marshmallow as mm
+    _need(orc.ref_post_available("god_ray") and orc.ref_post_available("radial_blur")
+          and orc.ref_post_available("tonemap"))
+    w, h = 320, 180
+    u = mm.scene.uniforms(w, h, yaw=yaw, pitch=12.0, sun_elevation=elev)
+    src = sg.pattern(h, w, 21)
+    g = orc.post_pass("god_rays", u, src)
+    rg = orc.ref_post("god_ray", u, src)
+    assert np.all(np.abs(g - rg) <= _post_bound(src, [0, 1, 2, 3]))
+    b = orc.post_pass("radial_blur", u, g)
+    rb = orc.ref_post("radial_blur", u, g)
+    assert np.all(np.abs(b - rb) <= 0.5 * _post_bound(g, [0, 1, 2, 3]) + 1e-6 * np.abs(rb))
+    t = orc.post_tonemap(src).astype(int)
+    rt = orc.unorm8(orc.ref_post("tonemap", None, src)).astype(int)
+    d = np.abs(t[..., :3] - rt[..., :3])
+    assert d.max() <= 1 and (d > 0).mean() <= 1e-3
+
+
+@pytest.mark.parametrize("elev,time,yaw", [(30.0, 0.0, 0.0), (15.0, 300.0, 60.0), (60.0, 40.0, 0.0)])
+def test_shadow_matches_reference_shader_build(orc, elev, time, yaw):
+    import marshmallow as mm
+    import marshmallow.lib as L
+    _need(orc.ref_model_available())
+    w, h = 160, 90
+    u = mm.scene.uniforms(w, h, eye=(0.0, 150.0, 0.0), yaw=yaw, pitch=-20.0, sun_elevation=elev, time=time)
+    g = mm.scene.terrain_gbuffer(u, w, h)
+    tex = {"low_res": orc.noise(L.NOISE_LOWRES, 0, 64, 64, 64, 4),
+           "weather": orc.noise(L.NOISE_WEATHER, 0, 256, 256, 1, 4)[0]}
+    wp = g.reshape(-1, 4)
+    wp = wp[wp[:, 3] != 0]
+    got = orc.shadow(u, tex, wp)
+    want = orc.ref_model_shadow(u, tex, wp)
+    fin = np.isfinite(want)
+    assert (got > 0).mean() > 0.2
+    assert np.abs(got[fin] - want[fin]).max() <= 1e-6
+    assert np.all(got[~fin] >= 0.5 - 1e-6)

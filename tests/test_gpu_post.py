@@ -154,7 +154,7 @@ def test_exact_passes_vs_reference_shader_golden(cuda, env):
     b = cuda.full_like(src, -1.0)
     r.radial_blur(u, g, b, math=L.MATH_EXACT)
     out8 = cuda.zeros((h, w, 4), dtype=cuda.uint8, device="cuda")
-    r.tonemap(src, out8, math=L.MATH_EXACT)
+    r.tonemap(src, out8, math=L.MATH_EXACT, bgra=0)
     cuda.cuda.synchronize()
     g_np, b_np, t_np = g.cpu().numpy(), b.cpu().numpy(), out8.cpu().numpy()
     bound_a = 3e-5 * np.abs(src_np[..., 3]).max() + 1e-7

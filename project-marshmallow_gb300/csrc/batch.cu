@@ -117,8 +117,8 @@ __global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_MARCH_MIN_BLOCKS) batc
     const int r = local / blocks_x;
     const int by = r < p.row_split ? p.row_split - 1 - r : r;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int px = (local % blocks_x) * kBlockTileW + (warp % (kBlockTileW / 8)) * 8 + (lane & 7);
-    const int py = by * kBlockTileH + (warp / (kBlockTileW / 8)) * 4 + (lane >> 3);
+    const int px = tile_px(local % blocks_x, warp, lane);
+    const int py = tile_py(by, warp, lane);
     if (px >= p.width || py >= p.height) return;
     const Frame f = make_frame<false>(p);
     Work w;

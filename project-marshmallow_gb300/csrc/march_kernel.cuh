@@ -403,9 +403,13 @@ __device__ __forceinline__ float cloud_test(const MarchLaunch& p, const Frame& f
 
 // cloudHiRes (:214-228) in three stages: curl fetch, displaced hi-res fetch, erosion.
 template <bool E, int S>
-__device__ __forceinline__ V3 hires_point(const MarchLaunch& p, const Geo& g, float curlStrength) {
+__device__ __forceinline__ F4 curl_fetch(const MarchLaunch& p, const Geo& g) {
+    return sample2d<E, S>(p.curl, 0.0001f * g.sp.x, 0.0001f * g.sp.z);
+}
+
+template <bool E>
+__device__ __forceinline__ V3 curl_displace(const Geo& g, float curlStrength, const F4& c) {
     const V3 pos = g.sp;
-    const F4 c = sample2d<E, S>(p.curl, 0.0001f * pos.x, 0.0001f * pos.z);
     if (E) {
         V3 curl = {2.0f * c.x - 1.0f, 2.0f * c.y - 1.0f, 2.0f * c.z - 1.0f};
         return pos + 1.9f * curlStrength * curl;
@@ -413,6 +417,11 @@ __device__ __forceinline__ V3 hires_point(const MarchLaunch& p, const Geo& g, fl
         const float k = 1.9f * curlStrength;
         return {pos.x + k * (2.0f * c.x - 1.0f), pos.y + k * (2.0f * c.y - 1.0f), pos.z + k * (2.0f * c.z - 1.0f)};
     }
+}
+
+template <bool E, int S>
+__device__ __forceinline__ V3 hires_point(const MarchLaunch& p, const Geo& g, float curlStrength) {
+    return curl_displace<E>(g, curlStrength, curl_fetch<E, S>(p, g));
 }
 
 template <bool E, int S>
@@ -714,11 +723,28 @@ __device__ __forceinline__ void march_pixel(const MarchLaunch& p, const Frame& f
     store_pixel(p, px, py, composite<E>(p.u, f, r.rd, r.bg, r.alpha, accum, transmittance), firstT);
 }
 
-// Ray-tile order: each warp marches an 8x4 pixel sub-tile, so one warp's 32 rays are a compact
-// footprint in the density textures; a block of MM_TILED_WARPS warps covers 32x8 (8 warps) or
-// 16x8 (4 warps) pixels.
-constexpr int kBlockTileW = MM_TILED_WARPS == 8 ? 32 : 16;
-constexpr int kBlockTileH = 8;
+
+// Ray-tile order: each warp marches a kWarpTileW x (32 / kWarpTileW) pixel sub-tile (8x4 by
+// default), so one warp's 32 rays are a compact footprint in the density textures; the warps of a
+// block sit side by side across a block tile kBlockTileW wide (16 pixels for 4 warps, 32 for 8, or
+// one warp tile if that is wider) and stack down it.
+#ifndef MM_WARP_TILE_W
+#define MM_WARP_TILE_W 8
+#endif
+constexpr int kWarpTileW = MM_WARP_TILE_W;
+constexpr int kWarpTileH = 32 / kWarpTileW;
+static_assert(kWarpTileW == 4 || kWarpTileW == 8 || kWarpTileW == 16 || kWarpTileW == 32, "warp tile width");
+constexpr int kBlockTileW = (MM_TILED_WARPS == 8 ? 32 : 16) > kWarpTileW ? (MM_TILED_WARPS == 8 ? 32 : 16) : kWarpTileW;
+constexpr int kWarpsAcross = kBlockTileW / kWarpTileW;
+constexpr int kBlockTileH = kWarpTileH * (MM_TILED_WARPS / kWarpsAcross);
+
+// Pixel (before the 1/16-phase mapping) of a lane of a warp in block tile (bx, by).
+__device__ __forceinline__ int tile_px(int bx, int warp, int lane) {
+    return bx * kBlockTileW + (warp % kWarpsAcross) * kWarpTileW + lane % kWarpTileW;
+}
+__device__ __forceinline__ int tile_py(int by, int warp, int lane) {
+    return by * kBlockTileH + (warp / kWarpsAcross) * kWarpTileH + lane / kWarpTileW;
+}
 
 // Three variants of the same march, chosen per launch:
 //  - full frames: one cone tap at a time (G = 1) keeps registers low enough for 10 blocks per SM,
@@ -744,6 +770,7 @@ constexpr int kBlockTileH = 8;
 #ifndef MM_LATENCY_MIN_BLOCKS
 #define MM_LATENCY_MIN_BLOCKS 3
 #endif
+
 constexpr long long kLatencyRays = 262144;
 
 template <bool E, int S, bool C, int G, bool SC>
@@ -753,8 +780,8 @@ __device__ __forceinline__ void march_tiled_body(const MarchLaunch& p) {
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int by = (int)blockIdx.y < p.row_split ? p.row_split - 1 - (int)blockIdx.y : (int)blockIdx.y;
-    const int tx = blockIdx.x * kBlockTileW + (warp % (kBlockTileW / 8)) * 8 + (lane & 7);
-    const int ty = by * kBlockTileH + (warp / (kBlockTileW / 8)) * 4 + (lane >> 3);
+    const int tx = tile_px((int)blockIdx.x, warp, lane);
+    const int ty = tile_py(by, warp, lane);
     int px, py;
     if (p.pixel_mode == MM_PIXELS_PHASE16) {  // :292-298 (thread grid covers ceil(W/4) x ceil(H/4))
         px = tx * 4 + (p.phase % 4);

@@ -126,8 +126,8 @@ __global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_SUR_MIN_BLOCKS) march_
     cone_offsets(p.u, s_cone);
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int px = blockIdx.x * kBlockTileW + (warp % (kBlockTileW / 8)) * 8 + (lane & 7);
-    const int py = blockIdx.y * kBlockTileH + (warp / (kBlockTileW / 8)) * 4 + (lane >> 3);
+    const int px = tile_px((int)blockIdx.x, warp, lane);
+    const int py = tile_py((int)blockIdx.y, warp, lane);
     if (px >= p.width || py >= p.height) return;
     const Frame f = make_frame<false>(p);
     Work w;

@@ -301,7 +301,7 @@ __device__ __forceinline__ void cone_offsets(const mm_uniforms& u, V3* out) {
 //    the camera's x and z (:357-358), so proj.xz - cam.xz = R * d2.xz / |d2| with d2 = sp - c,
 //    i.e. 9 * d2.xz * rsqrt(|d2|^2).
 //  - remap/remapClamped with constant bounds folded into one multiply-add; the three layer
-//    profiles of cloudLayerDensity (:193-204) as 25 h (0.9 - h), 10 h (0.7 - h), 100 h (0.3 - h).
+//    profiles of cloudLayerDensity (:193-204) as h (22.5 - 25 h), h (7 - 10 h), h (30 - 100 h).
 //  - cloudTest's low-res fetch is skipped where the layer density is exactly zero (the product
 //    layer * remapClamped(...) is zero whatever the texel holds, :240, :243).
 
@@ -335,9 +335,9 @@ __device__ __forceinline__ Geo geo_at(const Frame& f, V3 pos) {
 }
 
 __device__ __forceinline__ float layer_fast(float h, float type) {
-    const float cumulus = fmaxf(0.0f, 25.0f * h * (0.9f - h));
-    const float strato = fmaxf(0.0f, 10.0f * h * (0.7f - h));
-    const float stratus = fmaxf(0.0f, 100.0f * h * (0.3f - h));
+    const float cumulus = fmaxf(0.0f, h * (22.5f - 25.0f * h));
+    const float strato = fmaxf(0.0f, h * (7.0f - 10.0f * h));
+    const float stratus = fmaxf(0.0f, h * (30.0f - 100.0f * h));
     const float d1 = stratus + (strato - stratus) * __saturatef(type * 2.0f);
     const float d2 = strato + (cumulus - strato) * __saturatef(type * 2.0f - 1.0f);
     return d1 + (d2 - d1) * type;

@@ -22,6 +22,10 @@ NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexp
                       "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", os.path.join(REPO, "include")]
 # Units whose results must equal the CPU oracle bit for bit: no FMA contraction.
 EXACT_UNITS = {"march_exact.cu", "noise.cu", "reproject.cu", "shadow_exact.cu", "post_exact.cu"}
+# Production-arithmetic units (gated against the FP64 oracle, not bit-exact): FP32 denormals are
+# flushed to zero, which drops the denormal handling around the SFU operations (rsqrt, rcp, ex2,
+# lg2) from the march's dependent chains.
+FAST_UNITS = {"march_fast.cu", "surrogate.cu", "batch.cu", "reproject_fast.cu", "shadow.cu", "post.cu"}
 CUDA_UNITS = ["api.cu", "march_fast.cu", "march_exact.cu", "noise.cu", "peaks.cu", "noalloc.cu", "mlp.cu", "surrogate.cu", "batch.cu", "reproject.cu", "reproject_fast.cu", "shadow.cu", "shadow_exact.cu", "post.cu", "post_exact.cu"]
 CXX_UNITS = ["scene.cpp", "assets.cpp"]
 HEADERS = ["mm_internal.h", "mm_math.h", "march_kernel.cuh", "tc.cuh", "shadow_kernel.cuh", "post_kernel.cuh"]
@@ -45,6 +49,8 @@ def _cmd_for(unit, obj):
         flags = list(NVCC_COMMON) + _extra_flags()
         if unit in EXACT_UNITS:
             flags += ["-fmad=false"]
+        if unit in FAST_UNITS:
+            flags += ["-ftz=true"]
         return [nvcc()] + flags + ["-c", src, "-o", obj]
     return ["g++", "-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-Wall",
             "-I", os.path.join(REPO, "include"), "-c", src, "-o", obj]
@@ -57,7 +63,7 @@ def _digest():
             h.update(name.encode() + b"\0" + f.read())
     with open(os.path.join(REPO, "include", "mm.h"), "rb") as f:
         h.update(f.read())
-    h.update(" ".join(NVCC_COMMON + sorted(EXACT_UNITS) + _extra_flags()).encode())
+    h.update(" ".join(NVCC_COMMON + sorted(EXACT_UNITS) + sorted(FAST_UNITS) + _extra_flags()).encode())
     h.update(os.uname().machine.encode())
     return h.hexdigest()
 

@@ -750,19 +750,21 @@ __device__ __forceinline__ int tile_py(int by, int warp, int lane) {
 //  - full frames: one cone tap at a time (G = 1) keeps registers low enough for 10 blocks per SM,
 //    and the texture unit is kept busy by the many warps;
 //  - launches of at most kLatencyRays rays (a 1920x1080 frame at 1/16 of its pixels, or a small
-//    image): such a launch is bounded below by the latency of its longest rays (~1000 dependent
-//    fetch rounds just above the horizon, ~0.6 ms on GB300 whatever the launch size), so all six
-//    sun-cone taps of a sample are issued together (G = 6: a sample's cone takes 3 dependent fetch
-//    rounds instead of up to 18) at 3 blocks per SM for the registers;
-//  - larger 1/16-pixel launches (3840x2160/16: several waves): cone taps in pairs (G = 2, 7 blocks).
-// Measured over the 16-frame sweep (mean of frames 0, 5, 10, 15): 1920x1080/16 0.67 ms (G = 1),
-// 0.58 (G = 2), 0.50 (G = 6); 3840x2160/16 0.65 (G = 1), 0.60 (G = 2), 0.73 (G = 6).  Issuing the
-// curl fetch speculatively with the cloudTest fetches (SC) did not help.
+//    image): such a launch is bounded below by the latency of its longest rays (a few hundred
+//    dependent samples just above the horizon, ~0.5 ms on GB300 whatever the launch size), so all
+//    six sun-cone taps of a sample are issued together (G = 6: a sample's cone takes 3 dependent
+//    fetch rounds instead of up to 18) at 3 blocks per SM for the registers;
+//  - larger 1/16-pixel launches (3840x2160/16: several waves): cone taps in threes (G = 3, 6 blocks).
+// Measured over the 16-frame sweep (mean of frames 0, 5, 10, 15; production units built with
+// denormals flushed): 1920x1080/16 0.48 ms (G = 6); 3840x2160/16 0.68 (G = 1, 10 blocks), 0.56
+// (G = 2, 7 or 8 blocks), 0.53 (G = 3, 6 blocks), 0.54 / 0.56 (G = 3, 5 / 7 blocks), 0.60 / 0.67
+// (G = 6, 4 / 3 blocks).  Issuing the curl fetch speculatively with the cloudTest fetches (SC) did
+// not help.
 #ifndef MM_PHASE16_CONE_GROUP
-#define MM_PHASE16_CONE_GROUP 2
+#define MM_PHASE16_CONE_GROUP 3
 #endif
 #ifndef MM_PHASE16_MIN_BLOCKS
-#define MM_PHASE16_MIN_BLOCKS 7
+#define MM_PHASE16_MIN_BLOCKS 6
 #endif
 #ifndef MM_PHASE16_SPEC_CURL
 #define MM_PHASE16_SPEC_CURL 0

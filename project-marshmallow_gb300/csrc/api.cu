@@ -500,6 +500,7 @@ void mm::fill_march_launch(const mm_uniforms& u, const mm_scene_textures* tex, c
     p.uv_h = o.ref_uv_1080p ? 1080.0f : (float)out.height;
     p.coverage_offset = o.coverage_offset;
     p.counters = reinterpret_cast<unsigned long long*>(o.d_counters);
+    march_host_consts(p);
 }
 
 extern "C" {

@@ -260,14 +260,18 @@ __device__ __forceinline__ Frame make_frame(const MarchLaunch& p) {
     f.center.y = -kRadius * 0.5f * 0.995f;  // :357-358
     f.wind = ld3(u.sky.wind);
     f.time = u.sky.wind[3];  // :289
-    f.sunDir = normalize<E>(ld3(u.sun.direction_basis + 4));  // :324
+    if (E)
+        f.sunDir = normalize<E>(ld3(u.sun.direction_basis + 4));  // :324
+    else
+        f.sunDir = ld3(p.sun_dir);
     f.sunY = u.sun.direction[1];
     f.thickness = 0.5f * kRadius * 0.02f;  // :360
     f.coverage_offset = p.coverage_offset;
-    f.wind20 = 20.0f * f.wind;
+    f.wind20 = E ? 20.0f * f.wind : ld3(p.wind20);
     f.wscale20 = {2.0f, 1.0f, 0.0f};
     return f;
 }
+
 
 // Cone offsets mat3(directionBasis) * v (:392-401), computed once per block into shared memory
 // by threads 0..5 (the caller synchronizes).
@@ -455,7 +459,15 @@ __device__ __forceinline__ float cloud_hires(const MarchLaunch& p, const Geo& g,
 
 // Sun-cone taps i0 .. i0+G-1 of one sample (:441-453): their fetches are issued together; the
 // densities are added to densityAlongLight in tap order.
-template <bool E, int S, int G>
+// Cone offset k: from the block's shared copy, or (PC: production path, the cone loop unrolled so k
+// is a constant) from the launch parameters, where the host put it.
+template <bool E, bool PC>
+__device__ __forceinline__ V3 cone_offset(const MarchLaunch& p, const V3* cone, int k) {
+    if (!E && PC) return {p.cone[3 * k], p.cone[3 * k + 1], p.cone[3 * k + 2]};
+    return cone[k];
+}
+
+template <bool E, int S, int G, bool PC = false>
 __device__ __forceinline__ float cone_taps(const MarchLaunch& p, const Frame& f, const V3* cone, int i0, V3 pos,
                                            float stepSize, float dal, unsigned long long& n_test,
                                            unsigned long long& n_hires) {
@@ -463,7 +475,7 @@ __device__ __forceinline__ float cone_taps(const MarchLaunch& p, const Frame& f,
     TestFetch c[G];
 #pragma unroll
     for (int j = 0; j < G; ++j) {
-        g[j] = geo_at<E>(f, pos + 3.0f * stepSize * cone[i0 + j]);
+        g[j] = geo_at<E>(f, pos + 3.0f * stepSize * cone_offset<E, PC>(p, cone, i0 + j));
         c[j] = test_fetch<E, S>(p, f, g[j]);
     }
     float d[G];
@@ -658,7 +670,8 @@ __device__ __forceinline__ void flush_work(unsigned long long* cnt, const Work& 
 // G = cone taps whose fetches are issued together (the densities are still added in tap order);
 // SC = in small-step mode, issue the sample's curl fetch with its cloudTest fetches (speculative:
 // used only if the sample has density).
-template <bool E, int S, int G = MM_CONE_GROUP, bool SC = (MM_SPEC_CURL != 0)>
+// PC = cone offsets from the launch parameters with the cone loop unrolled (see cone_offset).
+template <bool E, int S, int G = MM_CONE_GROUP, bool SC = (MM_SPEC_CURL != 0), bool PC = false>
 __device__ __forceinline__ void march_pixel(const MarchLaunch& p, const Frame& f, const V3* cone, int px, int py,
                                             Work& w) {
     const Ray r = ray_setup<E, S>(p, f, px, py);
@@ -699,10 +712,17 @@ __device__ __forceinline__ void march_pixel(const MarchLaunch& p, const Frame& f
                 density = cloud_hires<E, S>(p, g, stepSize, density, w.hires);
             if (density < 0.0001f) continue;
             float densityAlongLight = 0.0f;
+            if constexpr (!E && PC) {
+#pragma unroll
+                for (int i = 0; i < 6; i += G)
+                    densityAlongLight = cone_taps<E, S, G, true>(p, f, cone, i, pos, stepSize, densityAlongLight,
+                                                                 w.test, w.hires);
+            } else {
 #pragma unroll 1
-            for (int i = 0; i < 6; i += G)
-                densityAlongLight = cone_taps<E, S, G>(p, f, cone, i, pos, stepSize, densityAlongLight, w.test,
-                                                       w.hires);
+                for (int i = 0; i < 6; i += G)
+                    densityAlongLight = cone_taps<E, S, G>(p, f, cone, i, pos, stepSize, densityAlongLight, w.test,
+                                                           w.hires);
+            }
             transmittance = shade<E>(transmittance, accum, densityAlongLight, loDensity, g.rh, r.cosTheta, r.hg);
             ++w.acc;
             if (firstT == CUDART_INF_F) firstT = t;
@@ -775,7 +795,7 @@ __device__ __forceinline__ int tile_py(int by, int warp, int lane) {
 
 constexpr long long kLatencyRays = 262144;
 
-template <bool E, int S, bool C, int G, bool SC>
+template <bool E, int S, bool C, int G, bool SC, bool PC = false>
 __device__ __forceinline__ void march_tiled_body(const MarchLaunch& p) {
     __shared__ V3 s_cone[6];
     cone_offsets(p.u, s_cone);
@@ -795,7 +815,7 @@ __device__ __forceinline__ void march_tiled_body(const MarchLaunch& p) {
     if (px >= p.width || py >= p.height) return;  // :301 with the runtime image size
     const Frame f = make_frame<E>(p);
     Work w;  // work counts; dead code unless C (counters requested)
-    march_pixel<E, S, G, SC>(p, f, s_cone, px, py, w);
+    march_pixel<E, S, G, SC, PC>(p, f, s_cone, px, py, w);
     if (C) flush_work(p.counters, w);
 }
 
@@ -806,12 +826,12 @@ __global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_MARCH_MIN_BLOCKS) marc
 
 template <bool E, int S, bool C>
 __global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_PHASE16_MIN_BLOCKS) march_tiled_phase16_kernel(MarchLaunch p) {
-    march_tiled_body<E, S, C, MM_PHASE16_CONE_GROUP, (MM_PHASE16_SPEC_CURL != 0)>(p);
+    march_tiled_body<E, S, C, MM_PHASE16_CONE_GROUP, (MM_PHASE16_SPEC_CURL != 0), true>(p);
 }
 
 template <bool E, int S, bool C>
 __global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_LATENCY_MIN_BLOCKS) march_tiled_latency_kernel(MarchLaunch p) {
-    march_tiled_body<E, S, C, 6, false>(p);
+    march_tiled_body<E, S, C, 6, false, true>(p);
 }
 
 // Launch order of the block rows.  A ray's cost grows as it nears the horizon (it crosses more of

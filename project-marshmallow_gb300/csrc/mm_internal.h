@@ -5,6 +5,8 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <math.h>
+
 #include "../../include/mm.h"
 
 #if defined(MM_HAVE_CUDA_RUNTIME) || defined(__CUDACC__)
@@ -89,6 +91,11 @@ struct MarchLaunch {
     float coverage_offset;
     unsigned long long* counters;
     int row_split;  // tiled march: block rows [0, row_split) run in reverse order first (0 = launch order)
+    // Per-frame constants of the production-arithmetic march, computed once on the host
+    // (march_host_consts) so the kernels read them from the parameter bank instead of holding them
+    // in registers: the normalized sun direction and 20 * wind.
+    float sun_dir[3], wind20[3];
+    float cone[18];  // the six sun-cone offsets mat3(directionBasis) * v (compute-clouds.comp:392-401)
 };
 
 // Kernel launchers (one translation unit per arithmetic mode).
@@ -117,6 +124,23 @@ TexView texture_view(mm_texture t);
 // Argument contract of mm_clouds_march and the kernel record of one view (api.cu).
 int validate_march(mm_context ctx, const mm_uniforms* u, const mm_scene_textures* tex, const mm_image* out,
                    const mm_march_options* opt);
+// Host side of the production frame constants (make_frame<false> reads them): normalize(sun
+// direction basis column 1) and 20 * wind.
+inline void march_host_consts(MarchLaunch& p) {
+    const float* b = p.u.sun.direction_basis + 4;
+    const float inv = 1.0f / sqrtf((b[0] * b[0] + b[1] * b[1]) + b[2] * b[2]);
+    for (int i = 0; i < 3; ++i) {
+        p.sun_dir[i] = b[i] * inv;
+        p.wind20[i] = 20.0f * p.u.sky.wind[i];
+    }
+    static const float v[6][3] = {{0.0f, 0.6f, 0.0f}, {0.0f, 0.5f, 0.05f}, {0.1f, 0.75f, 0.0f},
+                                  {0.2f, 2.5f, 0.3f}, {0.0f, 6.0f, 0.0f},  {-0.1f, 1.0f, -0.2f}};
+    const float* m = p.u.sun.direction_basis;
+    for (int k = 0; k < 6; ++k)
+        for (int r = 0; r < 3; ++r)
+            p.cone[3 * k + r] = (m[r] * v[k][0] + m[4 + r] * v[k][1]) + m[8 + r] * v[k][2];
+}
+
 void fill_march_launch(const mm_uniforms& u, const mm_scene_textures* tex, const mm_image& out,
                        const mm_march_options& o, MarchLaunch* p);
 void batch_state_destroy(mm_context ctx);

@@ -387,15 +387,20 @@ __device__ __forceinline__ float test_finish(const Frame& f, const Geo& g, const
         erosion = remapClamped<E>(erosion, coverage, 1.0f, 0.0f, 1.0f);
         return remapClamped<E>(density, erosion, 1.0f, 0.0f, 1.0f);
     } else {
-        const float layer = layer_fast(g.rh, c.type);
-        const float density = layer * __saturatef(c.dn.x * (1.0f / 0.7f) - (0.3f / 0.7f));
-        if (!(density >= 0.0001f)) return 0.0f;
+        // Branch-free: the coverage and erosion terms are evaluated for every sample and the
+        // shader's early return (:243) becomes a select.  A divergent branch costs more here than
+        // the arithmetic it would skip (4K frame 3.41 -> 3.34 ms with this form).  For rh == 0 the
+        // power is exp2(-inf) = 0 and a zero divisor gives a NaN or infinity that __saturatef and
+        // the select turn into the shader's value.
+        const float n = __saturatef(c.dn.x * (1.0f / 0.7f) - (0.3f / 0.7f));
+        const float density = layer_fast(g.rh, c.type) * n;
         const float h = fminf(0.85f, c.cov + f.coverage_offset);
         const float e = clampf(1.0f - (h - 0.7f) * 2.0f, 0.8f, 1.0f);
-        const float coverage = e == 1.0f ? g.rh : exp2f(e * __log2f(g.rh));
+        const float coverage = exp2f(e * __log2f(g.rh));
         const float ero = 0.625f * c.dn.y + 0.25f * c.dn.z + 0.125f * c.dn.w;
         const float erosion = __saturatef((ero - coverage) * __fdividef(1.0f, 1.0f - coverage));
-        return __saturatef((density - erosion) * __fdividef(1.0f, 1.0f - erosion));
+        const float out = __saturatef((density - erosion) * __fdividef(1.0f, 1.0f - erosion));
+        return density >= 0.0001f ? out : 0.0f;
     }
 }
 
@@ -481,17 +486,36 @@ __device__ __forceinline__ float cone_taps(const MarchLaunch& p, const Frame& f,
     float d[G];
 #pragma unroll
     for (int j = 0; j < G; ++j) d[j] = test_finish<E>(f, g[j], c[j], n_test);
-    V3 q[G];
+    if constexpr (!E) {
+        // Production path: nearly every tap has density (144 M of 150 M per 4K frame), so the
+        // cloudHiRes of every tap is evaluated and added where the tap's density is positive, without
+        // a branch (4K frame 3.34 -> 3.25 ms; the 1/16-pixel launches ~15% faster).
+        V3 q[G];
 #pragma unroll
-    for (int j = 0; j < G; ++j)
-        if (d[j] > 0.0f) q[j] = hires_point<E, S>(p, g[j], stepSize);
-    F4 hv[G];
+        for (int j = 0; j < G; ++j) q[j] = hires_point<E, S>(p, g[j], stepSize);
+        F4 hv[G];
 #pragma unroll
-    for (int j = 0; j < G; ++j)
-        if (d[j] > 0.0f) hv[j] = hires_fetch<E, S>(p, q[j]);
+        for (int j = 0; j < G; ++j) hv[j] = hires_fetch<E, S>(p, q[j]);
 #pragma unroll
-    for (int j = 0; j < G; ++j)
-        if (d[j] > 0.0f) dal += hires_finish<E>(hv[j], g[j].rh, d[j], n_hires);
+        for (int j = 0; j < G; ++j) {
+            unsigned long long used = 0;
+            const float h = hires_finish<E>(hv[j], g[j].rh, d[j], used);
+            n_hires += d[j] > 0.0f ? used : 0ull;
+            dal += d[j] > 0.0f ? h : 0.0f;
+        }
+    } else {
+        V3 q[G];
+#pragma unroll
+        for (int j = 0; j < G; ++j)
+            if (d[j] > 0.0f) q[j] = hires_point<E, S>(p, g[j], stepSize);
+        F4 hv[G];
+#pragma unroll
+        for (int j = 0; j < G; ++j)
+            if (d[j] > 0.0f) hv[j] = hires_fetch<E, S>(p, q[j]);
+#pragma unroll
+        for (int j = 0; j < G; ++j)
+            if (d[j] > 0.0f) dal += hires_finish<E>(hv[j], g[j].rh, d[j], n_hires);
+    }
     return dal;
 }
 
@@ -780,6 +804,9 @@ __device__ __forceinline__ int tile_py(int by, int warp, int lane) {
 // (G = 2, 7 or 8 blocks), 0.53 (G = 3, 6 blocks), 0.54 / 0.56 (G = 3, 5 / 7 blocks), 0.60 / 0.67
 // (G = 6, 4 / 3 blocks).  Issuing the curl fetch speculatively with the cloudTest fetches (SC) did
 // not help.
+#ifndef MM_TILED_PARAM_CONE
+#define MM_TILED_PARAM_CONE 0  // full frames: cone offsets from the launch parameters, cone loop unrolled
+#endif
 #ifndef MM_PHASE16_CONE_GROUP
 #define MM_PHASE16_CONE_GROUP 3
 #endif
@@ -821,7 +848,7 @@ __device__ __forceinline__ void march_tiled_body(const MarchLaunch& p) {
 
 template <bool E, int S, bool C>
 __global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_MARCH_MIN_BLOCKS) march_tiled_kernel(MarchLaunch p) {
-    march_tiled_body<E, S, C, MM_CONE_GROUP, (MM_SPEC_CURL != 0)>(p);
+    march_tiled_body<E, S, C, MM_CONE_GROUP, (MM_SPEC_CURL != 0), (MM_TILED_PARAM_CONE != 0)>(p);
 }
 
 template <bool E, int S, bool C>

@@ -91,13 +91,16 @@ __device__ __forceinline__ float cloudTest(const ShadowLaunch& p, V3 center, V3 
     const float layer = layerDensity<E>(rh, info.z);
     const F4 n = march::sample3d<E, S>(p.low, 0.000057f * pos);
     float density = layer * march::remapClamped<E>(n.x, 0.3f, 1.0f, 0.0f, 1.0f);
-    if (density < 0.0001f) return 0.0f;
+    // The production path evaluates the tail for every sample and turns the early return (:118)
+    // into a select, as the march does (a divergent branch costs more than the arithmetic).
+    if (E && density < 0.0001f) return 0.0f;
     // heightBiasCoverage(relativeHeight, min(0.85, weather.r)), arguments swapped as in the shader (:120)
     const float h = fminf(0.85f, info.x + p.coverage_offset);
     const float coverage = M<E>::pow(rh, clampf(march::remap<E>(h, 0.7f, 0.8f, 1.0f, 0.6f), 0.6f, 1.0f));
     float erosion = (0.625f * n.y + 0.25f * n.z) + 0.125f * n.w;
     erosion = march::remapClamped<E>(erosion, coverage, 1.0f, 0.0f, 1.0f);
-    return march::remapClamped<E>(density, erosion, 1.0f, 0.0f, 1.0f);
+    const float out = march::remapClamped<E>(density, erosion, 1.0f, 0.0f, 1.0f);
+    return density < 0.0001f ? 0.0f : out;
 }
 
 template <bool E, int S>

@@ -331,8 +331,8 @@ int mm_clouds_frame(mm_context ctx, const mm_uniforms* u, const mm_scene_texture
                     const mm_image* out, const mm_march_options* opt, void* stream);
 
 /* ------------------------------------------------------------------------------------------ */
-/* Mesh cloud shadows: the low-res march of the mesh fragment shader (model.frag:52-130,       */
-/* 229-276), run over a G-buffer instead of rasterized fragments.                             */
+/* Mesh cloud shadows: the low-res march of the mesh fragment shader (model.frag:52-162,       */
+/* 221-222, 240-276), run over a G-buffer instead of rasterized fragments.                    */
 /* ------------------------------------------------------------------------------------------ */
 
 /* Per pixel, the world position of the mesh fragment that covers it (model.vert:39,

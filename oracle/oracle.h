@@ -78,7 +78,7 @@ uint32_t oracle_hash3(int32_t x, int32_t y, int32_t z, uint32_t s);
 int oracle_reproject_f32(const mm_uniforms* u, const float* src_rgba, const float* src_depth, int w, int h,
                          float* dst_rgba, float* dst_depth);
 
-/* Cloud shadow of the mesh pass (model.frag:52-130, 229-276) for n G-buffer pixels: world_pos holds
+/* Cloud shadow of the mesh pass (model.frag:52-162, 221-222, 240-276) for n G-buffer pixels: world_pos holds
  * float4 (xyz world position, w != 0 where a mesh fragment covers the pixel); out_shadow gets the
  * accumulated density (0 on uncovered pixels).  coverage_offset is added to weather.r, as in the march. */
 int oracle_shadow_f32(const mm_uniforms* u, const oracle_textures* t, const float* world_pos, size_t n,

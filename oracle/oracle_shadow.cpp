@@ -1,20 +1,20 @@
 // oracle_shadow.cpp - CPU restatement of the cloud-shadow march of the mesh pass,
-// SkyEngine/SkyEngine/Shaders/model.frag:52-130 and :229-276 (test infrastructure only).
+// SkyEngine/SkyEngine/Shaders/model.frag:52-162, :221-222 and :240-276 (test infrastructure only).
 //
 // The mesh fragment shader marches six low-res density samples from the fragment towards the sun
 // and darkens the fragment by the largest density it meets.  Its density model is a copy of
 // compute-clouds.comp's with other constants, kept here as the shader has them:
 //  - ATMOSPHERE_RADIUS 1e6 (:61; the sphere radius is half of it, raySphereIntersection uses 0.25),
-//    earth centre y = -0.5 * 0.99 * 1e6 (:243), shell thickness 0.5 * 1e6 * 0.02 = 10 km (:245);
+//    earth centre y = -0.5 * 0.99 * 1e6 (:245), shell thickness 0.5 * 1e6 * 0.02 = 10 km (:247);
 //  - weather coordinate 0.00001 * (proj.xz - camera.xz), low-res coordinate 0.000057 * pos (:109, :112);
 //  - cloudLayerDensity's second blend goes from stratocumulus to *stratus* (:95) and cumulus, though
 //    computed, is unused; cumulus fades over 0.7..1.0 (:90);
 //  - heightBiasCoverage gets its arguments swapped, as in the march (:120);
-//  - wind 20 * (wind.xyz + (0, 0.2 rh, 0)) * (wind.w + 200 rh) (:258);
-//  - the march runs along L, the sun direction in *view* space (:229-230), from 4 * fragPositionWC
-//    (:254), starting at t = the world-space intersection parameter of the quirk shared with the
-//    march (isect.t = length(p_world - ro_normalized), :158), stepping 0.1 * thickness (:250);
-//  - the shadow is max over the samples (:264), 1 once above 0.99 (:266-269).
+//  - wind 20 * (wind.xyz + (0, 0.2 rh, 0)) * (wind.w + 200 rh) (:265);
+//  - the march runs along L, the sun direction in *view* space (:221-222), from 4 * fragPositionWC
+//    (:257), starting at t = the world-space intersection parameter of the quirk shared with the
+//    march (isect.t = length(p_world - ro_normalized), :158), stepping 0.1 * thickness (:253);
+//  - the shadow is max over the samples (:269), 1 once above 0.99 (:271-274).
 // raySphereIntersection leaves isect.t unset when the sun ray misses the inner sphere (a fragment
 // above the cloud floor looking away from it); t = 0 is used there, here and on the GPU.
 //
@@ -105,21 +105,21 @@ struct Shadow {
         cam = {(T)u->camera.camera_position[0], (T)u->camera.camera_position[1], (T)u->camera.camera_position[2]};
         const float* b = u->sun.direction_basis + 4;  // directionBasis[1]
         db1 = {(T)b[0], (T)b[1], (T)b[2]};
-        // L = normalize((camera.view * vec4(directionBasis[1], 0)).xyz), flipped below -0.05 (:229-230)
+        // L = normalize((camera.view * vec4(directionBasis[1], 0)).xyz), flipped below -0.05 (:221-222)
         V3<T> l = {((T)v[0] * db1.x + (T)v[4] * db1.y) + (T)v[8] * db1.z,
                    ((T)v[1] * db1.x + (T)v[5] * db1.y) + (T)v[9] * db1.z,
                    ((T)v[2] * db1.x + (T)v[6] * db1.y) + (T)v[10] * db1.z};
         L = normalize(l);
         if (L.y < T(-0.05)) L = L * T(-1);
         center = cam;
-        center.y = -T(kRadius) * T(0.5) * T(0.99);  // :243
-        thickness = T(0.5) * T(kRadius) * T(0.02);    // :245
-        step = T(0.1) * thickness;                    // :250
+        center.y = -T(kRadius) * T(0.5) * T(0.99);  // :245
+        thickness = T(0.5) * T(kRadius) * T(0.02);    // :247
+        step = T(0.1) * thickness;                    // :253
         wind = {(T)u->sky.wind[0], (T)u->sky.wind[1], (T)u->sky.wind[2]};
         time = (T)u->sky.wind[3];
     }
 
-    // :246-272 for the fragment at world position wc
+    // :249-276 for the fragment at world position wc
     T shadow(V3<T> wc) const {
         T t = sphereT(wc, db1, center, T(kRadius));
         T accum = T(0);

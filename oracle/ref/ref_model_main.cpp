@@ -3,7 +3,7 @@
 // infrastructure: builds oracle/_ref/libref_model.so).
 //
 // The shader lights a fragment and then darkens it by the cloud shadow it marches:
-// color *= 1 - 2 * accumDensity, clamped at 0 (model.frag:229-285).  The shadow is not an output of
+// color *= 1 - 2 * accumDensity, clamped at 0 (model.frag:283-284).  The shadow is not an output of
 // the shader, so each fragment is shaded twice, with the caller's low-res cloud texture and with an
 // all-zero one (density 0, so accumDensity = 0); the caller recovers accumDensity from the ratio of
 // the two colours wherever the shadowed colour is not clamped (accumDensity < 0.5).

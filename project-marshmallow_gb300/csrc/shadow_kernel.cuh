@@ -1,10 +1,10 @@
-// shadow_kernel.cuh - the cloud-shadow march of the mesh pass (model.frag:52-130, 229-276) as CUDA
+// shadow_kernel.cuh - the cloud-shadow march of the mesh pass (model.frag:52-162, 221-222, 240-276) as CUDA
 // device code over a G-buffer of world positions.
 //
 // One thread per G-buffer pixel: the sun ray from the fragment meets the inner atmosphere sphere
 // (the start parameter t, with the march's isect.t quirk, :158), then up to six low-res density
-// samples march from 4 * fragPositionWC along L, the sun direction in view space (:229-230, :254),
-// 1 km apart (:250); the shadow is the largest density met, 1 once above 0.99 (:264-269).  The
+// samples march from 4 * fragPositionWC along L, the sun direction in view space (:221-222, :257),
+// 1 km apart (:253); the shadow is the largest density met, 1 once above 0.99 (:269-274).  The
 // density model has the mesh shader's own constants (radius 1e6, weather scale 1e-5, low-res
 // scale 5.7e-5, wind 20 (wind + (0, 0.2 rh, 0)) (t + 200 rh)) and its cloudLayerDensity, whose
 // second blend goes to stratus, not cumulus (:95).  Where the sun ray misses the inner sphere the
@@ -27,7 +27,7 @@ struct ShadowLaunch {
     size_t pos_pitch;  // bytes
     float* shadow;     // may be null
     size_t shadow_pitch;
-    float4* rgba;      // may be null: lit mesh colour darkened in place (model.frag:275-277)
+    float4* rgba;      // may be null: lit mesh colour darkened in place (model.frag:283-284)
     size_t rgba_pitch;
     int width, height;
     float coverage_offset;
@@ -81,7 +81,7 @@ __device__ __forceinline__ float cloudTest(const ShadowLaunch& p, V3 center, V3 
         u = 0.00001f * (proj.x - cam.x);
         v = 0.00001f * (proj.z - cam.z);
     } else {
-        // proj.xz - camera.xz = R * d.xz / |d| (the centre shares the camera's x and z, :242-243)
+        // proj.xz - camera.xz = R * d.xz / |d| (the centre shares the camera's x and z, :244-245)
         const V3 d = pos - center;
         const float k = 5.0f * rsqrtf(march::dot(d, d));
         u = d.x * k;

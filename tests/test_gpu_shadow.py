@@ -1,4 +1,4 @@
-"""The mesh cloud-shadow march (model.frag:52-130, 229-276) on the GPU against the CPU restatement."""
+"""The mesh cloud-shadow march (model.frag:52-162, 221-222, 240-276) on the GPU against the CPU restatement."""
 import ctypes as C
 
 import numpy as np

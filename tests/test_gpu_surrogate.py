@@ -8,7 +8,7 @@ What the test shows (printed, and bounded so regressions are caught):
   - training gain: held-out MSE of the predicted transmittance drops >= 8x from the untrained net;
   - frame error of the surrogate march vs the FP64 oracle and vs the plain march, and its time vs the
     plain march.  Measured on GB300: RMSE 2.0-3.4/255 (above the 2/255 gate of the method) and
-    ~1.1 ms slower per 4K frame; the assertion only bounds it at 5/255 so a broken pipeline fails.
+    0.8-1.4 ms slower per 4K frame; the assertion only bounds it at 5/255 so a broken pipeline fails.
 """
 import ctypes as C
 

@@ -717,9 +717,10 @@ __device__ __forceinline__ void march_pixel(const MarchLaunch& p, const Frame& f
         const V3 pos = f.cam + t * rd;
         const Geo g = geo_at<E>(f, pos);
         // Once the ray marches in small steps, a sample that finds density goes on to cloudHiRes;
-        // with SC its curl fetch is issued with the cloudTest fetches so the two latencies overlap.
-        V3 qh;
-        if (SC && !noHits) qh = hires_point<E, S>(p, g, stepSize);
+        // with SC its curl fetch is issued before the cloudTest fetches (and used after them), so a
+        // sample with density waits two dependent fetch rounds instead of three.
+        F4 cu;
+        if (SC && !noHits) cu = curl_fetch<E, S>(p, g);
         float density = cloud_test<E, S>(p, f, g, w.test);
         const float loDensity = density;
         if (density > 0.0f) {
@@ -731,7 +732,8 @@ __device__ __forceinline__ void march_pixel(const MarchLaunch& p, const Frame& f
                 continue;
             }
             if (SC)
-                density = hires_finish<E>(hires_fetch<E, S>(p, qh), g.rh, density, w.hires);
+                density = hires_finish<E>(hires_fetch<E, S>(p, curl_displace<E>(g, stepSize, cu)), g.rh, density,
+                                          w.hires);
             else
                 density = cloud_hires<E, S>(p, g, stepSize, density, w.hires);
             if (density < 0.0001f) continue;
@@ -802,8 +804,11 @@ __device__ __forceinline__ int tile_py(int by, int warp, int lane) {
 // Measured over the 16-frame sweep (mean of frames 0, 5, 10, 15; production units built with
 // denormals flushed): 1920x1080/16 0.48 ms (G = 6); 3840x2160/16 0.68 (G = 1, 10 blocks), 0.56
 // (G = 2, 7 or 8 blocks), 0.53 (G = 3, 6 blocks), 0.54 / 0.56 (G = 3, 5 / 7 blocks), 0.60 / 0.67
-// (G = 6, 4 / 3 blocks).  Issuing the curl fetch speculatively with the cloudTest fetches (SC) did
-// not help.
+// (G = 6, 4 / 3 blocks).  Both small-launch variants issue a small-step sample's curl fetch ahead of
+// its cloudTest fetches (SC): the longest rays are chains of small-step samples whose density is then
+// eroded away by cloudHiRes (~170 of their ~700 dependent fetch rounds), and SC takes one round out
+// of each: 1920x1080/16 0.35 -> 0.32 ms, 3840x2160/16 0.42 -> 0.41 ms.  Full frames, bound by
+// throughput, lose by the wasted fetches (3.24 -> 3.28 ms) and keep it off.
 #ifndef MM_TILED_PARAM_CONE
 #define MM_TILED_PARAM_CONE 0  // full frames: cone offsets from the launch parameters, cone loop unrolled
 #endif
@@ -814,7 +819,10 @@ __device__ __forceinline__ int tile_py(int by, int warp, int lane) {
 #define MM_PHASE16_MIN_BLOCKS 6
 #endif
 #ifndef MM_PHASE16_SPEC_CURL
-#define MM_PHASE16_SPEC_CURL 0
+#define MM_PHASE16_SPEC_CURL 1
+#endif
+#ifndef MM_LATENCY_SPEC_CURL
+#define MM_LATENCY_SPEC_CURL 1
 #endif
 #ifndef MM_LATENCY_MIN_BLOCKS
 #define MM_LATENCY_MIN_BLOCKS 3
@@ -858,7 +866,7 @@ __global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_PHASE16_MIN_BLOCKS) ma
 
 template <bool E, int S, bool C>
 __global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_LATENCY_MIN_BLOCKS) march_tiled_latency_kernel(MarchLaunch p) {
-    march_tiled_body<E, S, C, 6, false, true>(p);
+    march_tiled_body<E, S, C, 6, (MM_LATENCY_SPEC_CURL != 0), true>(p);
 }
 
 // Launch order of the block rows.  A ray's cost grows as it nears the horizon (it crosses more of

@@ -110,3 +110,22 @@ def test_camera_matches_reference_camera(mmlib):
         assert np.abs(p - rp).max() <= 1e-6 * np.abs(rp).max(), rec
         assert abs(u.camera.camera_params[0] - rec["aspect"][0]) <= 1e-7 * rec["aspect"][0]
         assert abs(u.camera.camera_params[1] - rec["tan_half_fov"][0]) <= 1e-7 * rec["tan_half_fov"][0]
+
+
+def test_plain_c_host_builds_and_runs(tmp_path, mmlib):
+    # The header compiles as C99 and a C host links libmm.so and calls the host-only entry points
+    # (tests/c_host/abi_host.c); no device is needed for these.
+    import shutil
+    import subprocess
+    from marshmallow import build as mb
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        import pytest
+        pytest.skip("no C compiler")
+    exe = str(tmp_path / "abi_host")
+    lib_dir = os.path.dirname(mb.LIB)
+    subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", os.path.join(REPO, "include"),
+                    os.path.join(REPO, "tests", "c_host", "abi_host.c"), "-L", lib_dir, "-l:libmm.so",
+                    "-Wl,-rpath," + lib_dir, "-o", exe], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout + r.stderr

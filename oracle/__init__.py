@@ -141,21 +141,31 @@ def ref_clouds_available():
     return os.path.exists(REF_CLOUDS_LIB)
 
 
-def ref_clouds_march(uniforms, textures, xs, ys, nthreads=0):
+def ref_clouds_mm_available():
+    """True where its build with mm_math.h's elementary functions exists as well."""
+    return os.path.exists(REF_CLOUDS_LIB.replace("libref_clouds.so", "libref_clouds_mm.so"))
+
+
+def ref_clouds_march(uniforms, textures, xs, ys, nthreads=0, mm_math=False):
     """The reference shader itself (compiled from its GLSL on the CPU) at pixels (xs[i], ys[i]) of the
-    1920 x 1080 frame it hard-codes; every pixel must be in the phase int(sun.color.a).  Returns rgba (n, 4)."""
+    1920 x 1080 frame it hard-codes; every pixel must be in the phase int(sun.color.a).  Returns rgba (n, 4).
+    mm_math: the build whose exp/pow/acos/cos/sin are mm_math.h's (the restatement's), else the C library's."""
     global _ref_clouds
     if _ref_clouds is None:
-        lib = C.CDLL(REF_CLOUDS_LIB)
+        _ref_clouds = {}
+    key = bool(mm_math)
+    if key not in _ref_clouds:
+        lib = C.CDLL(REF_CLOUDS_LIB.replace("libref_clouds.so", "libref_clouds_mm.so") if key else REF_CLOUDS_LIB)
         lib.ref_clouds_march.argtypes = [C.c_void_p, C.POINTER(OracleTextures), C.c_void_p, C.c_void_p, C.c_size_t,
                                          C.c_void_p, C.c_int]
-        _ref_clouds = lib
+        _ref_clouds[key] = lib
+    lib = _ref_clouds[key]
     keep, t = _textures(textures)
     xs = np.ascontiguousarray(xs, np.int32)
     ys = np.ascontiguousarray(ys, np.int32)
     out = np.zeros((len(xs), 4), np.float32)
-    rc = _ref_clouds.ref_clouds_march(C.addressof(uniforms), C.byref(t), xs.ctypes.data, ys.ctypes.data, len(xs),
-                                      out.ctypes.data, nthreads)
+    rc = lib.ref_clouds_march(C.addressof(uniforms), C.byref(t), xs.ctypes.data, ys.ctypes.data, len(xs),
+                              out.ctypes.data, nthreads)
     if rc:
         raise RuntimeError("ref_clouds_march failed: %d" % rc)
     return out

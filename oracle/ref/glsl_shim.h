@@ -11,8 +11,8 @@
 //    host thread at a time); `in`/`inout` parameter qualifiers vanish (the shaders read their
 //    inout parameters back nowhere);
 //  - vec/mat types and the built-in functions are glm's (swizzles included), with float overloads
-//    for the calls GLSL makes with integer literals (clamp(x, 0, 1) and the like) and the implicit
-//    int -> float conversion of mixed vector arithmetic;
+//    for the calls GLSL makes with integer literals (clamp(x, 0, 1) and the like), the implicit
+//    int -> float conversion of mixed vector arithmetic, and mix in the specification's form;
 //  - samplers: LINEAR filter with float weights, REPEAT or CLAMP_TO_EDGE, mip 0, on UNORM8 or float
 //    texels — the definition shared with the CPU restatement (x = u*N - 0.5, i0 = floor(x),
 //    a = x - i0, interpolated along x, then y, then z);
@@ -45,7 +45,17 @@ thread_local uvec3 gl_GlobalInvocationID;
 inline float clamp(float x, float a, float b) { return glm::clamp(x, a, b); }
 inline float min(float a, float b) { return glm::min(a, b); }
 inline float max(float a, float b) { return glm::max(a, b); }
-inline float mix(float a, float b, float t) { return glm::mix(a, b, t); }
+// mix as the GLSL specification defines it, x * (1 - a) + y * a (glm computes x + a * (y - x), which
+// differs in the last bit)
+inline float mix(float a, float b, float t) { return a * (1.0f - t) + b * t; }
+template <length_t L>
+inline vec<L, float> mix(const vec<L, float>& x, const vec<L, float>& y, float a) {
+    return x * (1.0f - a) + y * a;
+}
+template <length_t L>
+inline vec<L, float> mix(const vec<L, float>& x, const vec<L, float>& y, const vec<L, float>& a) {
+    return x * (vec<L, float>(1.0f) - a) + y * a;
+}
 inline float smoothstep(float e0, float e1, float x) { return glm::smoothstep(e0, e1, x); }
 
 // GLSL converts an integer vector operand to float implicitly (vec2(uv) / ivec2(dim)); glm does not.
@@ -144,3 +154,39 @@ inline vec4 imageLoad(const image2D& im, ivec2 p) {
 }
 
 inline ivec2 imageSize(const image2D& im) { return ivec2(im.w, im.h); }
+
+// ---------------------------------------------------------------------------------- elementary functions
+//
+// With GLSL_SHIM_MM_MATH the shader's exp, pow, acos, cos and sin are those of mm_math.h (the
+// functions the CPU restatement's float instance and the GPU's exact mode use) instead of the C
+// library's.  GLSL leaves their precision to the implementation, so either is the shader; with the
+// same functions on both sides every remaining difference would be one of arithmetic or order.
+#ifdef GLSL_SHIM_MM_MATH
+#include "mm_math.h"
+
+namespace glsl_mm {
+inline float pow_(float x, float y) { return mmx::mm_powf(x, y); }
+inline float exp_(float x) { return mmx::mm_expf(x); }
+inline float acos_(float x) { return mmx::mm_acosf(x); }
+inline float cos_(float x) { return mmx::mm_cosf(x); }
+inline float sin_(float x) { return mmx::mm_sinf(x); }
+template <length_t L>
+inline vec<L, float> pow_(const vec<L, float>& x, const vec<L, float>& y) {
+    vec<L, float> r;
+    for (length_t i = 0; i < L; ++i) r[i] = mmx::mm_powf(x[i], y[i]);
+    return r;
+}
+template <length_t L>
+inline vec<L, float> exp_(const vec<L, float>& x) {
+    vec<L, float> r;
+    for (length_t i = 0; i < L; ++i) r[i] = mmx::mm_expf(x[i]);
+    return r;
+}
+}  // namespace glsl_mm
+
+#define pow glsl_mm::pow_
+#define exp glsl_mm::exp_
+#define acos glsl_mm::acos_
+#define cos glsl_mm::cos_
+#define sin glsl_mm::sin_
+#endif

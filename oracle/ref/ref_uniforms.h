@@ -14,6 +14,11 @@
 #undef in
 #undef inout
 #undef out
+#undef pow
+#undef exp
+#undef acos
+#undef cos
+#undef sin
 
 #include <atomic>
 #include <cstring>

@@ -17,6 +17,10 @@
                       seed-0 generator textures: for five frames (sweep poses, a low sun, a night sky;
                       pixel phases 0, 5, 10, 15, 3) the rgba of every 32nd pixel of the phase in x and y
                       of its hard-coded 1920x1080 frame, with the uniform blocks that made them.
+  shader_clouds_mm.json  the same five frames from the shader built with mm_math.h's exp, pow, acos,
+                      cos and sin (the restatement's elementary functions): SHA-256 of the rgba of every
+                      8th pixel of the phase in x and y, which the FP32 restatement and the GPU's exact
+                      kernel reproduce bit for bit.
   shader_passes.npz   the reference's reproject.comp, model.frag, god-ray.frag, radialBlur.frag and
                       tonemap.frag compiled the same way: SHA-256 of the reprojected images of three
                       camera motions (tests/shader_golden.py REPROJECT_CASES, seeded hash images);
@@ -80,6 +84,7 @@ def asset_digests(se):
 
 
 SHADER_STRIDE = 32
+SHADER_MM_STRIDE = 8
 
 
 def shader_frames():
@@ -128,6 +133,18 @@ def shader_clouds_golden():
         images.append(rgba)
     np.savez_compressed(os.path.join(HERE, "shader_clouds_1080p.npz"), names=np.array(names),
                         uniforms=np.stack(ublocks), rgba=np.stack(images), stride=SHADER_STRIDE)
+
+    import hashlib
+    mm_frames = []
+    for name, u, night in shader_frames():
+        t = dict(tex, night_sky=night)
+        rows, cols = shader_pixels(int(u.sun.color[3]), SHADER_MM_STRIDE)
+        ys, xs = np.meshgrid(rows, cols, indexing="ij")
+        rgba = oracle.ref_clouds_march(u, t, xs.ravel(), ys.ravel(), mm_math=True).reshape(len(rows), len(cols), 4)
+        mm_frames.append({"name": name, "uniforms": C.string_at(C.addressof(u), C.sizeof(u)).hex(),
+                          "sha256": hashlib.sha256(np.ascontiguousarray(rgba, np.float32).tobytes()).hexdigest()})
+    with open(os.path.join(HERE, "shader_clouds_mm.json"), "w") as f:
+        json.dump({"stride": SHADER_MM_STRIDE, "frames": mm_frames}, f, indent=1)
 
 
 def shader_passes_golden():

@@ -94,3 +94,24 @@ def digest(a):
 def passes():
     z = np.load(PASSES)
     return {k: z[k] for k in z.files}
+
+
+# The same frames from the shader built with mm_math.h's elementary functions: SHA-256 digests of the
+# rgba of every 8th pixel of the phase (tests/golden/shader_clouds_mm.json), reproduced bit for bit by
+# the FP32 restatement and the GPU's exact kernel.
+MM_GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "shader_clouds_mm.json")
+
+
+def mm_frames():
+    """[(name, uniforms, rows, cols, sha256)]"""
+    import json
+    import marshmallow.lib as L
+    z = json.load(open(MM_GOLDEN))
+    stride = int(z["stride"])
+    out = []
+    for fr in z["frames"]:
+        u = L.Uniforms.from_buffer_copy(bytes.fromhex(fr["uniforms"]))
+        phase = int(u.sun.color[3])
+        out.append((fr["name"], u, np.arange(phase // 4, 1080, stride), np.arange(phase % 4, 1920, stride),
+                    fr["sha256"]))
+    return out

@@ -196,6 +196,23 @@ def test_vs_reference_shader_golden(cuda, orc, renderer, gpu_textures, mode):
     night.close()
 
 
+def test_exact_equals_reference_shader_with_the_same_elementary_functions(cuda, orc, renderer, gpu_textures):
+    # The reference shader built with mm_math.h's elementary functions, five frames, every 8th pixel of
+    # the phase: the exact kernel's rgba has the same SHA-256 (tests/golden/shader_clouds_mm.json).
+    import marshmallow as mm
+    import marshmallow.lib as L
+    import shader_golden as sg
+    night = mm.render.Textures.from_arrays({"night_sky": sg.night_sky(orc)})
+    handles = dict(gpu_textures.handles)
+    handles["night_sky"] = night.handles["night_sky"]
+    tex = mm.render.Textures(handles=handles)
+    for name, u, rows, cols, sha in sg.mm_frames():
+        rgba, _ = render(cuda, renderer, u, tex, 1920, 1080, depth=False, pixel_mode=L.PIXELS_PHASE16, ref_uv_1080p=1,
+                         sampler=L.SAMPLER_SOFTWARE, math=L.MATH_EXACT)
+        assert sg.digest(np.ascontiguousarray(rgba[rows][:, cols], np.float32)) == sha, name
+    night.close()
+
+
 def test_coverage_offset_and_sun_sweep(cuda, orc, renderer, gpu_textures, host_textures):
     import marshmallow as mm
     import marshmallow.lib as L

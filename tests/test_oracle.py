@@ -278,6 +278,23 @@ def test_oracle_matches_reference_shader_golden(orc, oracle_textures):
         assert e["nan"] == 0 and e["rmse_255"] <= 1.0 and e["p999_255"] <= 4.0 and e["frac_over_4"] <= 0.002, (name, e)
 
 
+def test_oracle_equals_reference_shader_with_the_same_elementary_functions(orc, oracle_textures):
+    # Built with mm_math.h's exp/pow/acos/cos/sin (the restatement's), the reference shader and the
+    # FP32 restatement agree bit for bit on every pixel of five frames: sky, clouds, night
+    # (tests/golden/shader_clouds_mm.json).  Every operation and its order is the shader's.
+    import shader_golden as sg
+    frames = sg.mm_frames()
+    assert len(frames) == 5
+    for name, u, rows, cols, sha in frames:
+        got = sg.oracle_march(orc, u, _shader_textures(orc, oracle_textures, u), rows, cols, 32)
+        assert sg.digest(np.ascontiguousarray(got, np.float32)) == sha, name
+        if orc.ref_clouds_mm_available():
+            ys, xs = np.meshgrid(rows, cols, indexing="ij")
+            ref = orc.ref_clouds_march(u, _shader_textures(orc, oracle_textures, u), xs.ravel(), ys.ravel(),
+                                       mm_math=True).reshape(got.shape)
+            assert np.array_equal(ref.view(np.uint32), got.view(np.uint32)), name
+
+
 def test_reference_shader_build_reproduces_golden(orc, oracle_textures):
     # Where the reference shader has been compiled (`make -C oracle ref`), it reproduces the fixture.
     import shader_golden as sg
@@ -330,6 +347,9 @@ def test_oracle_matches_reference_shader_on_shipped_textures(orc, mmlib):
         ref = orc.ref_clouds_march(u, t, xs.ravel(), ys.ravel()).reshape(len(rows), len(cols), 4)
         o32 = sg.oracle_march(orc, u, t, rows, cols, 32)
         assert sg.max_rel(o32, ref) <= 2e-4, pose
+        if orc.ref_clouds_mm_available():
+            ref_mm = orc.ref_clouds_march(u, t, xs.ravel(), ys.ravel(), mm_math=True).reshape(o32.shape)
+            assert np.array_equal(ref_mm.view(np.uint32), o32.view(np.uint32)), pose
 
 
 # The other passes against their shaders compiled the same way.  Reprojection is bit-identical (the

@@ -17,7 +17,8 @@
 //    texels — the definition shared with the CPU restatement (x = u*N - 0.5, i0 = floor(x),
 //    a = x - i0, interpolated along x, then y, then z);
 //  - images: imageStore / imageLoad / imageSize on float4 rows;
-//  - main() is renamed glsl_main(); gl_GlobalInvocationID is a thread_local the driver sets.
+//  - main() is renamed glsl_main(); gl_GlobalInvocationID is a thread_local that the harness
+//    (oracle/ref/ref_*_main.cpp) sets.
 #pragma once
 
 #define GLM_FORCE_SWIZZLE

@@ -31,7 +31,7 @@ for _p in (REPO, os.path.join(REPO, "project-marshmallow_gb300")):
 
 METRIC = "Mrays/s at 3840x2160 (cloud raymarch frame, every pixel marched)"
 SWEEP = 16
-PROFILE_SUMMARY = os.path.join(REPO, "profiles", "march_kernel_4k.txt")
+PROFILE_SUMMARY = os.path.join(REPO, "profiles", "march_dram_4k.txt")
 
 
 def parse_args():

@@ -157,15 +157,16 @@ int mm_noise_texel_bytes(const mm_noise_desc* desc, size_t* bytes);
 int mm_noise_fill(const mm_noise_desc* desc, void* d_texels, size_t bytes, void* stream);
 
 /* MM_NOISE_REF_CURL without any device allocation, for callers that cannot allocate when they
- * generate (an engine or plugin host that owns the whole device heap, work being recorded into a
- * CUDA graph, a frame loop that must not hit the allocator).  No counterpart in the reference,
+ * generate (an engine or plugin host that owns the whole device heap, a frame loop that must not
+ * hit the allocator).  No counterpart in the reference,
  * which generates this texture offline on the CPU.  Writes the same 128x128 RGBA8 texels as
  * mm_noise_fill with kind MM_NOISE_REF_CURL.  width/height: 0 or 128 (the maximum: sizes beyond
  * it are rejected with MM_ERR_INVALID_ARGUMENT).  Its scratch is one static device array of the
  * library (~192 KB, held by every GPU that loads the library until exit) shared by all calls:
  * calls whose GPU work overlaps (different streams, or threads) race on it and must be ordered by
  * the caller.  The first call on a device looks up the array's address on that device, so make it
- * before any stream capture; later calls only launch kernels. */
+ * before any stream capture; later calls only launch kernels.  The address is kept for the life of
+ * the process: calls after a device reset (cudaDeviceReset) are not supported. */
 int mm_noise_fill_ref_curl_noalloc(int width, int height, void* d_texels, size_t bytes, void* stream);
 
 /* Hash stage of the seeded generators, for bit-exactness checks: out[i] = hash3(x, y, z, s) for

@@ -28,7 +28,7 @@ class OracleTextures(C.Structure):
 class OracleFrame(C.Structure):
     _fields_ = [("width", C.c_int), ("height", C.c_int), ("pixel_mode", C.c_int), ("coverage_offset", C.c_float),
                 ("ref_uv_1080p", C.c_int), ("row_begin", C.c_int), ("row_end", C.c_int), ("row_step", C.c_int),
-                ("col_begin", C.c_int), ("col_step", C.c_int)]
+                ("col_begin", C.c_int), ("col_step", C.c_int), ("filter", C.c_int)]
 
 
 def build():
@@ -68,8 +68,35 @@ def load():
         lib.oracle_post_tonemap.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_size_t, C.c_int]
         lib.oracle_post_chain.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
                                           C.c_size_t, C.c_int]
+        lib.oracle_sample.argtypes = [C.POINTER(OracleTexture), C.c_int, C.c_void_p, C.c_size_t, C.c_int, C.c_void_p]
+        lib.oracle_uniforms.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int, C.c_float,
+                                        C.c_float, C.c_float, C.c_int, C.c_void_p]
         _lib = lib
     return _lib
+
+
+UNIFORM_FLOATS = 124  # the four std140 blocks of descriptor set 2, bindings 0-3 (496 bytes)
+
+
+def uniforms(width, height, eye=(0.0, 10.0, 0.0), yaw=0.0, pitch=15.0, fov=60.0, sun_elevation=30.0,
+             sun_azimuth=0.0, time=0.0, phase=0):
+    """The uniform blocks of one frame, built by the oracle's own restatement of the reference's
+    Camera and SkyManager (no CUDA library involved): a ctypes array of 124 floats in the std140
+    layout the march reads."""
+    u = (C.c_float * UNIFORM_FLOATS)()
+    e = (C.c_float * 3)(*eye)
+    rc = load().oracle_uniforms(e, yaw, pitch, fov, width, height, sun_elevation, sun_azimuth, time, phase,
+                                C.addressof(u))
+    if rc:
+        raise ValueError("oracle_uniforms: invalid arguments")
+    return u
+
+
+def sweep_uniforms(k, width, height, n=16, sun_elevation=30.0, sun_azimuth=0.0):
+    """Frame k of the camera sweep (yaw 0 -> 90 deg, pitch 5 -> 25 deg over n frames, t += 0.1 s)."""
+    f = k / float(n - 1) if n > 1 else 0.0
+    return uniforms(width, height, yaw=90.0 * f, pitch=5.0 + 20.0 * f, time=0.1 * k, sun_elevation=sun_elevation,
+                    sun_azimuth=sun_azimuth)
 
 
 def noise(kind, seed, w, h, d, channels):
@@ -98,8 +125,11 @@ def _tex(a):
     return OracleTexture(a.ctypes.data, a.shape[2], a.shape[1], a.shape[0], a.shape[3])
 
 
+FILTER_EXACT, FILTER_TEXTURE_UNIT = 0, 1
+
+
 def march(uniforms, textures, width, height, precision=32, pixel_mode=0, coverage_offset=0.0, ref_uv_1080p=0,
-          rows=None, col_begin=0, col_step=1, nthreads=0):
+          rows=None, col_begin=0, col_step=1, nthreads=0, filter=FILTER_EXACT):
     """Runs the oracle march over a pixel sample.
 
     textures: dict with weather (h,w,4), curl (h,w,2|4), low_res (d,h,w,4), hi_res (d,h,w,4), night_sky (opt).
@@ -111,7 +141,8 @@ def march(uniforms, textures, width, height, precision=32, pixel_mode=0, coverag
     t = OracleTextures(_tex(keep.get("weather")), _tex(keep.get("night_sky")), _tex(keep.get("curl")),
                        _tex(keep.get("low_res")), _tex(keep.get("hi_res")))
     rb, re_, rs = rows if rows else (0, height, 1)
-    f = OracleFrame(width, height, pixel_mode, coverage_offset, ref_uv_1080p, rb, re_, rs, col_begin, col_step)
+    f = OracleFrame(width, height, pixel_mode, coverage_offset, ref_uv_1080p, rb, re_, rs, col_begin, col_step,
+                    filter)
     n_rows = max(0, (re_ - rb + rs - 1) // rs)
     n_cols = max(0, (width - col_begin + col_step - 1) // col_step)
     rgba = np.zeros((n_rows, n_cols, 4), np.float32)
@@ -123,6 +154,20 @@ def march(uniforms, textures, width, height, precision=32, pixel_mode=0, coverag
     if rc:
         raise RuntimeError("oracle march failed: %d" % rc)
     return rgba, depth, cnt
+
+
+def sample(texels, coords, filter=FILTER_TEXTURE_UNIT):
+    """The oracle's sampler on a UNORM8 texture ((h, w, c) or (d, h, w, c)) at float32 normalized
+    coordinates (n, 2) or (n, 3): (n, 4) float32."""
+    texels = np.ascontiguousarray(texels, np.uint8)
+    coords = np.ascontiguousarray(coords, np.float32)
+    out = np.zeros((coords.shape[0], 4), np.float32)
+    t = _tex(texels)
+    rc = load().oracle_sample(C.byref(t), coords.shape[1], coords.ctypes.data, coords.shape[0], filter,
+                              out.ctypes.data)
+    if rc:
+        raise RuntimeError("oracle_sample failed: %d" % rc)
+    return out
 
 
 def _textures(textures):

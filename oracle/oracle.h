@@ -51,12 +51,18 @@ typedef struct oracle_frame {
     int ref_uv_1080p;
     int row_begin, row_end, row_step;
     int col_begin, col_step;
+    int filter; /* 0: exact filter weights; 1: the texture unit's 8-bit fixed-point filter */
 } oracle_frame;
 
 int oracle_march_f32(const mm_uniforms* u, const oracle_textures* t, const oracle_frame* f,
                      float* out_rgba, float* out_depth, uint64_t* counters, int nthreads);
 int oracle_march_f64(const mm_uniforms* u, const oracle_textures* t, const oracle_frame* f,
                      float* out_rgba, float* out_depth, uint64_t* counters, int nthreads);
+
+/* The texture unit's LINEAR/WRAP filter (oracle_glsl.h) of an oracle texture at n normalized
+ * coordinates: dims 2 reads (u, v) pairs, dims 3 (u, v, w) triples from coords; out gets 4 floats
+ * per fetch (channels the texture lacks read 0, 0, 1).  filter 0 uses exact float weights instead. */
+int oracle_sample(const oracle_texture* t, int dims, const float* coords, size_t n, int filter, float* out);
 
 /* ImageUtils.cpp GenerateCurlNoise: 128x128 RGBA8 (A = 255), rows top to bottom. */
 int oracle_ref_curl(uint8_t* out_rgba);
@@ -96,6 +102,14 @@ int oracle_post_radial_blur(const mm_uniforms* u, const float* src, int w, int h
 int oracle_post_tonemap(const float* src, int w, int h, uint8_t* out, size_t pitch, int bgra);
 int oracle_post_chain(const mm_uniforms* u, const float* clouds, const float* mesh, int w, int h, uint8_t* out,
                       size_t pitch, int bgra);
+
+/* The four uniform blocks as the reference's host fills them each frame: Camera (camera.cpp:27-39,
+ * 139-147; near 0.1, far 1000; proj[1][1] negated) looking along (cos yaw cos pitch, sin pitch,
+ * sin yaw cos pitch) with its m_forward the reverse of that, and SkyManager (SkyManager.cpp:15-100)
+ * for the sun at (cos el cos az, sin el, cos el sin az); wind time `time`, sun.color.a = pixel_phase.
+ * camera_prev = camera.  Returns 0, or 1 for invalid arguments. */
+int oracle_uniforms(const float eye[3], float yaw_deg, float pitch_deg, float fov_deg, int width, int height,
+                    float sun_elevation_deg, float sun_azimuth_deg, float time, int pixel_phase, mm_uniforms* u);
 
 /* Uncharted-2 tonemap of tonemap.frag:10-28 (exposure 0.7, white 50.2, gamma 1/2.2) applied to
  * n rgb triples (stride 4 floats), written as n*3 floats. */

@@ -16,7 +16,9 @@
 //  - samplers (Texture.cpp:29-52, 315-338: LINEAR, REPEAT, normalized coords, mip 0, UNORM8):
 //    x = u*N - 0.5, i0 = floor(x), a = x - i0, texel indices wrapped modulo N, value texel/255,
 //    interpolated along x, then y, then z with mix; channels a 2-channel texture lacks read
-//    (.., 0, 1) as Vulkan format conversion does.
+//    (.., 0, 1) as Vulkan format conversion does.  oracle_frame.filter = 1 replaces the exact
+//    weights with the texture unit's fixed-point filter (oracle_glsl.h), the filter the GPU
+//    applies to the same request.
 #include <math.h>
 #include <string.h>
 
@@ -43,6 +45,7 @@ struct March {
     const oracle_textures* tex;
     T coverage_offset;
     Counters* cnt;
+    int filter;  // 0: exact filter weights in T; 1: the texture unit's fixed-point filter
 
     // compute-clouds.comp:65-71
     static T remap(T v, T lo0, T hi0, T lo1, T hi1) { return lo1 + (((v - lo0) / (hi0 - lo0)) * (hi1 - lo1)); }
@@ -116,11 +119,11 @@ struct March {
     T cloudHiRes(V3<T> pos, T curlStrength, T origDensity, T rh) const {
         cnt->cloud_hires++;
         T c = T(0.0001);
-        V4<T> cs = sample2d<T>(tex->curl, c * pos.x, c * pos.z);
+        V4<T> cs = sample2d<T>(tex->curl, c * pos.x, c * pos.z, filter);
         V3<T> curl = {cs.x, cs.y, cs.z};
         curl = T(2) * curl - V3<T>{T(1), T(1), T(1)};
         pos = pos + T(1.9) * curlStrength * curl;
-        V4<T> dn = sample3d<T>(tex->hi_res, T(0.0004) * pos);
+        V4<T> dn = sample3d<T>(tex->hi_res, T(0.0004) * pos, filter);
         T erosion = T(0.625) * dn.x + T(0.25) * dn.y + T(0.125) * dn.z;
         erosion = mixT(erosion, T(1) - erosion, clampT(rh * T(10), T(0), T(1)));
         return remapClamped(origDensity, T(1) * erosion, T(1), T(0), T(1));
@@ -131,9 +134,9 @@ struct March {
         cnt->cloud_test++;
         V3<T> proj = projectedShellPoint(pos, center);
         V3<T> cam = v3(u->camera.camera_position);
-        V4<T> info = sample2d<T>(tex->weather, T(0.000009) * (proj.x - cam.x), T(0.000009) * (proj.z - cam.z));
+        V4<T> info = sample2d<T>(tex->weather, T(0.000009) * (proj.x - cam.x), T(0.000009) * (proj.z - cam.z), filter);
         T layer = cloudLayerDensity(rh, info.z);
-        V4<T> dn = sample3d<T>(tex->low_res, T(0.00002) * pos);
+        V4<T> dn = sample3d<T>(tex->low_res, T(0.00002) * pos, filter);
         T density = layer * remapClamped(dn.x, T(0.3), T(1), T(0), T(1));
         if (density < T(0.0001)) return T(0);
         T coverage = heightBiasCoverage(rh, Fn<T>::min(T(0.85), info.x + coverage_offset));
@@ -239,7 +242,7 @@ struct March {
             V3<T> point = outer.t * rrd + rro;
             V3<T> pp = projectedShellPoint(point, earthCenter);
             V4<T> ns = sample2d<T>(tex->night_sky, T(0.00002) * (pp.x - cameraPos.x) + T(0.35),
-                                   T(0.00002) * (pp.z - cameraPos.z) + T(0.35));
+                                   T(0.00002) * (pp.z - cameraPos.z) + T(0.35), filter);
             bg = {ns.x, ns.y, ns.z};
             bg = bg * (V3<T>{Fn<T>::sqrt(bg.x), Fn<T>::sqrt(bg.y), Fn<T>::sqrt(bg.z)} * T(0.75));
             bg = pow3(bg, T(2.2));
@@ -375,7 +378,7 @@ int run(const mm_uniforms* u, const oracle_textures* t, const oracle_frame* f, f
     std::vector<Counters> per(nthreads);
     std::atomic<int> next(0);
     auto worker = [&](int tid) {
-        March<T> m{u, t, (T)f->coverage_offset, &per[tid]};
+        March<T> m{u, t, (T)f->coverage_offset, &per[tid], f->filter};
         for (int r = next++; r < rows; r = next++) {
             int py = f->row_begin + r * f->row_step;
             for (int c = 0; c < cols; ++c) {
@@ -418,6 +421,22 @@ int oracle_march_f32(const mm_uniforms* u, const oracle_textures* t, const oracl
 int oracle_march_f64(const mm_uniforms* u, const oracle_textures* t, const oracle_frame* f,
                      float* out_rgba, float* out_depth, uint64_t* counters, int nthreads) {
     return run<double>(u, t, f, out_rgba, out_depth, counters, nthreads);
+}
+
+int oracle_sample(const oracle_texture* t, int dims, const float* coords, size_t n, int filter, float* out) {
+    if (!t || !t->texels || !coords || !out || (dims != 2 && dims != 3)) return MM_ERR_INVALID_ARGUMENT;
+    for (size_t i = 0; i < n; ++i) {
+        V4<float> v;
+        if (dims == 2)
+            v = sample2d<float>(*t, coords[2 * i], coords[2 * i + 1], filter);
+        else
+            v = sample3d<float>(*t, V3<float>{coords[3 * i], coords[3 * i + 1], coords[3 * i + 2]}, filter);
+        out[4 * i] = v.x;
+        out[4 * i + 1] = v.y;
+        out[4 * i + 2] = v.z;
+        out[4 * i + 3] = v.w;
+    }
+    return MM_OK;
 }
 
 // tonemap.frag:11-22 with the constants of :27-28 (exposure 0.7, white 50.2, gamma 1/2.2).

@@ -4,8 +4,7 @@
 // min/max before it can normalise them to 8 bits (ImageUtils.cpp:179-219), and allocates it on the
 // stream for every call.  Some callers cannot allocate device memory at that point: a render
 // engine or plugin host that reserves the whole device heap up front and hands out only its own
-// buffers, a caller recording the work into a CUDA graph, or a frame loop that must not risk the
-// allocator's synchronisation.  This entry point uses a fixed scratch array compiled into the
+// buffers, or a frame loop that must not risk the allocator's synchronisation.  This entry point uses a fixed scratch array compiled into the
 // library instead.  The array lives in every GPU that loads the library until the process exits.
 #include <cuda_runtime.h>
 
@@ -26,7 +25,9 @@ constexpr int kMaxDevices = 64;
 std::mutex g_mutex;
 float* g_scratch_ptr[kMaxDevices] = {};
 
-// Device address of the scratch array on the current device, looked up once per device.
+// Device address of the scratch array on the current device, looked up once per device and kept
+// for the life of the process.  A device reset (cudaDeviceReset) after the first call reloads the
+// module and may move the array; calling this entry point after such a reset is not supported.
 int scratch_for_current_device(float** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);

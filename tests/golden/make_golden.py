@@ -191,7 +191,9 @@ def shader_passes_golden():
 
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    ref = args[0] if args else "/root/reference"
+    ref = args[0] if args else os.environ.get("MM_REF_DIR", "")
+    if not os.path.isdir(os.path.join(ref, "SkyEngine")):
+        sys.exit("usage: make_golden.py <reference tree root>  (or set MM_REF_DIR)")
     se = os.path.join(ref, "SkyEngine", "SkyEngine")
     asset_digests(se)
     if "--digests-only" in sys.argv:

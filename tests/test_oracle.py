@@ -469,3 +469,50 @@ def test_shadow_matches_reference_shader_build(orc, elev, time, yaw):
     assert (got > 0).mean() > 0.2
     assert np.abs(got[fin] - want[fin]).max() <= 1e-6
     assert np.all(got[~fin] >= 0.5 - 1e-6)
+
+
+def test_oracle_uniforms_match_reference_camera_and_sky(orc):
+    # The oracle's own camera/sky set-up (used by the benchmark's reference arm, which must not load
+    # the CUDA library) against the reference's Camera and SkyManager compiled unchanged
+    # (tests/golden/camera_reference.json, sky_reference.json).
+    import math
+    recs = json.load(open(os.path.join(GOLDEN, "camera_reference.json")))
+    for rec in recs:
+        # the reference camera looks along -m_forward: the same camera is (yaw + 180, -pitch) here
+        u = np.frombuffer(orc.uniforms(rec["width"], rec["height"], eye=rec["eye"], yaw=rec["yaw"] + 180.0,
+                                       pitch=-rec["pitch"], fov=rec["fov"]), np.float32)
+        v, rv = u[0:16].astype(np.float64), np.array(rec["view"])
+        p, rp = u[16:32].astype(np.float64), np.array(rec["proj"])
+        assert np.abs(v - rv).max() <= 1e-6 * max(1.0, np.abs(rv).max()), rec
+        assert np.abs(p - rp).max() <= 1e-6 * np.abs(rp).max(), rec
+        assert abs(u[36] - rec["aspect"][0]) <= 1e-7 * rec["aspect"][0]
+        assert abs(u[37] - rec["tan_half_fov"][0]) <= 1e-7 * rec["tan_half_fov"][0]
+    sky = json.load(open(os.path.join(GOLDEN, "sky_reference.json")))
+    for r in sky:
+        # SkyManager.cpp:47-52 direction from its fractions, then as elevation/azimuth angles
+        th, ph = 2.0 * math.pi * (r["elevation"] - 0.5), 2.0 * math.pi * (r["azimuth"] - 0.5)
+        d = (math.cos(ph), math.sin(ph) * math.sin(th), math.sin(ph) * math.cos(th))
+        el, az = math.degrees(math.asin(max(-1.0, min(1.0, d[1])))), math.degrees(math.atan2(d[2], d[0]))
+        u = np.frombuffer(orc.uniforms(64, 64, sun_elevation=el, sun_azimuth=az, time=r["time"]), np.float32)
+        sun, sk = u[76:108], u[108:124]
+        np.testing.assert_allclose(sun[4:8], r["direction"], rtol=1e-5, atol=1e-6)
+        np.testing.assert_allclose(sun[0:4], r["location"], rtol=1e-5, atol=0.05)
+        np.testing.assert_allclose(sun[12:28], r["direction_basis"], rtol=1e-5, atol=2e-6)
+        np.testing.assert_allclose(sun[8:11], r["color_rgb"], rtol=1e-5)
+        np.testing.assert_allclose(sun[28], r["intensity"][0], rtol=1e-5, atol=1e-3)
+        np.testing.assert_allclose(sk[0:4], r["beta_r"], rtol=1e-5)
+        np.testing.assert_allclose(sk[8:12], r["wind"], rtol=1e-6)
+        np.testing.assert_allclose(sk[12], r["mie_directional"][0])
+
+
+def test_oracle_uniforms_equal_the_library_set_up(orc, mmlib):
+    # The same frames built by the library (scene.cpp) and by the oracle: identical bytes.
+    import ctypes as C
+    import marshmallow as mm
+    for k in range(16):
+        for w, h in ((3840, 2160), (256, 256)):
+            el = (30.0, 5.0, -6.0, 85.0)[k % 4]
+            a = np.frombuffer(orc.sweep_uniforms(k, w, h, sun_elevation=el), np.float32)
+            u = mm.scene.sweep_uniforms(k, w, h, sun_elevation=el)
+            b = np.frombuffer(C.string_at(C.addressof(u), 496), np.float32)
+            assert np.array_equal(a, b), (k, w, h)

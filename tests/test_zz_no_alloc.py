@@ -1,8 +1,7 @@
 """mm_noise_fill_ref_curl_noalloc: the reference curl generator with no device allocation.
 
 It serves callers that cannot allocate device memory when they generate: an engine that owns the
-whole device heap, work recorded into a CUDA graph, a frame loop that must not touch the
-allocator.  It must write exactly what the allocating entry point (mm_noise_fill with
+whole device heap, or a frame loop that must not touch the allocator.  It must write exactly what the allocating entry point (mm_noise_fill with
 MM_NOISE_REF_CURL) writes, call after call, although every call reuses the same static scratch
 array.  This file runs last so a failure here comes after every other test has run.
 """

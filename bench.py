@@ -49,6 +49,8 @@ def parse_args():
     ap.add_argument("--schedule", choices=["persistent", "tiled"], default="tiled")
     ap.add_argument("--density", choices=["unorm8", "fp16", "bf16"], default="unorm8")
     ap.add_argument("--no-passes", action="store_true", help="skip the timings of the other passes")
+    ap.add_argument("--no-variants", action="store_true",
+                    help="skip the metric's variants (FP16/BF16 density, surrogate cone)")
     ap.add_argument("--batch", action="store_true",
                     help="time the uneven-view batch (mm_clouds_march_batch) instead of the 4K frame")
     ap.add_argument("--batch-views", type=int, default=70, help="first N views of the 70-view batch")
@@ -144,6 +146,15 @@ def frame_uniforms(k, w, h):
     return mm.scene.sweep_uniforms(k % SWEEP, w, h, n=SWEEP)
 
 
+def bench_config(args, w, h):
+    """The workload both arms report (identical dicts, so the two lines describe the same config)."""
+    return {"workload": "cloud march %dx%d, plain FP32 march, %s-filtered %s density textures, 16-frame sweep"
+                        % (w, h, args.sampler, args.density.upper()),
+            "width": w, "height": h, "frames_cycled": SWEEP, "textures": "seed 0 (Perlin-Worley/Worley/curl/weather)",
+            "l2": "flushed between frames (256 MB memset outside the timed events)", "variant": "plain",
+            "math": args.math, "sampler": args.sampler, "density": args.density, "schedule": args.schedule}
+
+
 def cpu_march_sample(u, host_tex, w, h, row0, step):
     """FP32 oracle over rows row0::step and columns row0%step::step; returns (rays, seconds, threads)."""
     import oracle
@@ -155,45 +166,43 @@ def cpu_march_sample(u, host_tex, w, h, row0, step):
     return rgba.shape[0] * rgba.shape[1], dt, threads
 
 
-def oracle_textures():
-    import oracle
-    import marshmallow.lib as L
-    return {"low_res": oracle.noise(L.NOISE_LOWRES, 0, 128, 128, 128, 4),
-            "hi_res": oracle.noise(L.NOISE_HIRES, 0, 32, 32, 32, 4),
-            "curl": oracle.noise(L.NOISE_CURL2D, 0, 128, 128, 1, 2)[0],
-            "weather": oracle.noise(L.NOISE_WEATHER, 0, 512, 512, 1, 4)[0]}
-
-
 # ------------------------------------------------------------------------------ reference arm
 
 
 def run_reference(args):
+    """The reference's march on the host CPU: the FP32 restatement of compute-clouds.comp (the oracle)
+    over all host threads, with uniforms and textures from the oracle's own set-up (no GPU library is
+    loaded).  Each step marches 1/64 of one sweep frame (every 8th row and column, offset per step)."""
     rank, world, _ = rank_info()
     if rank != 0:
         return
     import oracle
     oracle.build()
     w, h = args.width, args.height
-    tex = oracle_textures()
-    step_px = 8  # each step: 1/64 of the frame (every 8th row and column), a bounded CPU sample
+    tex = oracle.seed_textures(0)
+    step_px = 8
     for k in range(args.warmup):
-        cpu_march_sample(frame_uniforms(k, w, h), tex, w, h, k % step_px, step_px)
+        cpu_march_sample(oracle.sweep_uniforms(k % SWEEP, w, h, n=SWEEP), tex, w, h, k % step_px, step_px)
     rays = 0
     secs = 0.0
     threads = 1
     for k in range(args.steps):
-        n, dt, threads = cpu_march_sample(frame_uniforms(k, w, h), tex, w, h, k % step_px, step_px)
+        n, dt, threads = cpu_march_sample(oracle.sweep_uniforms(k % SWEEP, w, h, n=SWEEP), tex, w, h, k % step_px,
+                                          step_px)
         rays += n
         secs += dt
     value = rays / secs / 1e6
+    sample = ("FP32 oracle restatement of compute-clouds.comp on %d host threads; each step marches every 8th row "
+              "and column of one sweep frame (1/64 of its rays, %d rays per step on average)"
+              % (threads, rays // max(1, args.steps)))
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mrays/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * secs / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "cloud march %dx%d, 16-frame sweep, seed-0 textures" % (w, h), "width": w,
-                   "height": h, "sample_per_step": "every 8th row and column of one frame (1/64 of its rays)"},
+        "config": bench_config(args, w, h),
+        "sample_per_step": "1/64 of a frame: every 8th row and column",
         "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
-                         "sample": "FP32 oracle restatement of compute-clouds.comp; per step 1/64 of a 4K frame"},
+                         "sample": sample},
         "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -413,6 +422,112 @@ def reference_frame_1080p(renderer, textures, flush, stream, frames=16):
                     % (100.0 * float((gbuf[..., 3] != 0).float().mean()))}
 
 
+# ------------------------------------------------------------------------------ the metric's variants
+
+
+def train_surrogate(lib, stream):
+    """The learned sun-cone surrogate as the library trains it: 2^22 samples of the plain six-tap cone
+    (texture seeds 1-8, sun 0-90 deg) by mm_surrogate_generate, then 2048 Adam steps of batch 16384
+    by mm_mlp_train on the tensor cores.  Returns the network and the training cost."""
+    import torch
+    import marshmallow.lib as L
+    sp = C.c_void_p(stream.cuda_stream)
+    per_seed = 1 << 19
+    x = torch.empty((8 * per_seed, 16), dtype=torch.bfloat16, device="cuda")
+    t = torch.empty(8 * per_seed, dtype=torch.float32, device="cuda")
+    n = C.c_int()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    L.check(lib.mm_surrogate_generate(1, 8, per_seed, 150000.0, C.c_void_p(x.data_ptr()), C.c_void_p(t.data_ptr()),
+                                      C.byref(n), sp), "mm_surrogate_generate")
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    net = C.c_void_p()
+    L.check(lib.mm_mlp_create(11, C.byref(net)), "mm_mlp_create")
+    steps = 0
+    for lr, k in ((3e-3, 1024), (1e-3, 1024)):
+        L.check(lib.mm_mlp_train(net, C.c_void_p(x.data_ptr()), C.c_void_p(t.data_ptr()), n.value, 16384, k, lr, None,
+                                 sp), "mm_mlp_train")
+        steps += k
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    return net, {"samples": n.value, "generate_ms": round(1e3 * (t1 - t0), 2), "train_steps": steps, "batch": 16384,
+                 "train_ms": round(1e3 * (t2 - t1), 2),
+                 "note": "one-off cost per texture set, not part of a frame"}
+
+
+def measure_variants(lib, renderer, textures, w, h, flush, stream, with_oracle):
+    """BASELINE's metric itself: the 3840x2160 sweep for each variant of the march -- plain with
+    UNORM8 (the reference's texel format), FP16 or BF16 density textures, and the learned
+    sun-cone surrogate with UNORM8 or FP16 density -- each with its ms/frame (CUDA events, L2 flushed
+    before every frame, mean over the 16 sweep frames) and its error against the FP64 oracle (exact
+    filter weights) on a fixed grid (every 8th row and column, sweep frames 0, 5, 10, 15)."""
+    import numpy as np
+    import torch
+    import marshmallow as mm
+    import marshmallow.lib as L
+    net, training = train_surrogate(lib, stream)
+    variants = [("plain_unorm8", L.FORMAT_UNORM8, None), ("surrogate_unorm8", L.FORMAT_UNORM8, net.value),
+                ("plain_fp16", L.FORMAT_FP16, None), ("surrogate_fp16", L.FORMAT_FP16, net.value),
+                ("plain_bf16", L.FORMAT_BF16, None)]
+    err_frames = (0, 5, 10, 15)
+    refs = {}
+    if with_oracle:
+        import oracle
+        oracle.build()
+        host = textures.host_all()
+        for k in err_frames:
+            ref, rdep, _ = oracle.march(frame_uniforms(k, w, h), host, w, h, precision=64, rows=(3, h, 8), col_begin=3,
+                                        col_step=8)
+            refs[k] = (ref, rdep)
+    rgba = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+    dep = torch.empty((h, w), dtype=torch.float32, device="cuda")
+    out = {}
+    try:
+        for name, fmt, sur in variants:
+            textures.set_density_format(fmt)
+            opts = dict(density_format=fmt, surrogate=sur)
+            for k in range(SWEEP):
+                renderer.march(frame_uniforms(k, w, h), textures, rgba, dep, **opts)
+            ts = []
+            for k in range(SWEEP):
+                flush.zero_()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                renderer.march(frame_uniforms(k, w, h), textures, rgba, dep, **opts)
+                b.record(stream)
+                torch.cuda.synchronize()
+                ts.append(a.elapsed_time(b))
+            ms = sum(ts) / len(ts)
+            d = {"ms_per_frame": round(ms, 4), "mrays_per_s": round(w * h / ms / 1e3, 1)}
+            if refs:
+                es = []
+                for k in err_frames:
+                    renderer.march(frame_uniforms(k, w, h), textures, rgba, dep, **opts)
+                    torch.cuda.synchronize()
+                    img = rgba[3::8, 3::8].cpu().numpy()
+                    dd = dep[3::8, 3::8].cpu().numpy()
+                    es.append(mm.metrics.frame_errors(img, refs[k][0], dd, refs[k][1]))
+                d.update({"rmse_255_mean": round(float(np.mean([e["rmse_255"] for e in es])), 4),
+                          "rmse_255_max": round(max(e["rmse_255"] for e in es), 4),
+                          "p999_255_max": round(max(e["p999_255"] for e in es), 3),
+                          "max_255_max": round(max(e["max_255"] for e in es), 2),
+                          "frac_over_4_max": max(e["frac_over_4"] for e in es),
+                          "depth_rel_median_max": max(e["depth_rel_median"] for e in es),
+                          "within_rmse_2_255": all(e["rmse_255"] <= 2.0 for e in es)})
+            out[name] = d
+    finally:
+        textures.set_density_format(L.FORMAT_UNORM8)
+        lib.mm_mlp_destroy(net)
+    plain = out["plain_unorm8"]["ms_per_frame"]
+    summary = {"surrogate_fp16_vs_plain_speedup": round(plain / out["surrogate_fp16"]["ms_per_frame"], 4),
+               "fp16_vs_plain_speedup": round(plain / out["plain_fp16"]["ms_per_frame"], 4),
+               "surrogate_fp16_rmse_255_max": out["surrogate_fp16"].get("rmse_255_max"),
+               "error_yardstick": "FP64 oracle, exact filter weights, every 8th row and column of sweep frames "
+                                  "0, 5, 10, 15" if refs else None}
+    return {"variants": out, "surrogate_training": training, "summary": summary}
+
+
 # ------------------------------------------------------------------------------ our arm
 
 
@@ -588,6 +703,10 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_passes:
         configs = measure_configs(renderer, textures, flush, stream, not args.no_cpu_baseline)
 
+    variants = None
+    if rank == 0 and world == 1 and not args.no_variants:
+        variants = measure_variants(lib, renderer, textures, w, h, flush, stream, not args.no_cpu_baseline)
+
     passes = None
     if rank == 0 and not args.no_passes:
         passes = measure_passes(renderer, textures, rgba, depth, uniforms, w, h, flush, stream, hbm_peak,
@@ -598,12 +717,7 @@ def run_ours(args):
             "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_frame, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "cloud march %dx%d, plain FP32, %s-filtered %s density textures, "
-                                   "16-frame sweep" % (w, h, args.sampler, args.density.upper()),
-                       "width": w, "height": h, "frames_cycled": SWEEP, "textures": "seed 0, generated on GPU",
-                       "l2": "flushed between frames (256 MB memset outside the timed events)",
-                       "variant": "plain", "math": args.math, "sampler": args.sampler, "density": args.density,
-                       "schedule": args.schedule},
+            "config": bench_config(args, w, h),
             "roofline": {"bound": "tex", "achieved": round(achieved_gfetch, 2), "peak": round(peak_eff, 1),
                          "unit": "Gfetch/s",
                          "frac": round(tex_time_frac, 4), "traffic": traffic,
@@ -620,7 +734,7 @@ def run_ours(args):
             "work_per_frame": {"cloud_test": n_test / args.steps, "cloud_hires": n_hires / args.steps,
                                "iterations": n_iter / args.steps, "accumulated": n_acc / args.steps},
             "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks, "cpu_baseline": cpu,
-            "configs": configs, "passes": passes,
+            "configs": configs, "variants": variants, "passes": passes,
         }
         print(json.dumps(line), flush=True)
     renderer.close()

@@ -215,6 +215,14 @@ int mm_texture_copy_to_host(mm_texture tex, void* dst, size_t bytes);
 /* Re-encodes the hardware-filtered copy of a texture in another mm_texel_format. */
 int mm_texture_set_format(mm_texture tex, int format, void* stream);
 
+/* Filtered fetches of a texture's hardware copy (the texture unit's LINEAR filter with WRAP
+ * addressing and normalized coordinates, as the march reads it) at n caller coordinates, for
+ * checking a filter model against the hardware: d_coords holds (u, v) pairs for a 2D texture or
+ * (u, v, w) triples for a 3D one, d_out receives 4 floats per fetch (channels the texture lacks
+ * read 0, 0, 1).  Device pointers; stream ordered.  Stands in for the GLSL texture() calls of
+ * compute-clouds.comp:218,223,236,238 on the bound samplers (Texture.cpp:29-52, 315-338). */
+int mm_texture_sample(mm_texture tex, const float* d_coords, size_t n, float* d_out, void* stream);
+
 int mm_texture_destroy(mm_texture tex);
 
 /* The five samplers of descriptor set 2 bindings 4..8 (compute-clouds.comp:43-47).

@@ -126,6 +126,14 @@ def _tex(a):
 
 
 FILTER_EXACT, FILTER_TEXTURE_UNIT = 0, 1
+# mm_noise_kind values of the seeded generators (include/mm.h)
+NOISE_LOWRES, NOISE_HIRES, NOISE_CURL2D, NOISE_WEATHER = 0, 1, 2, 3
+
+
+def seed_textures(seed=0):
+    """The four seeded textures of the benchmark scene from the oracle's own generators."""
+    return {"low_res": noise(NOISE_LOWRES, seed, 128, 128, 128, 4), "hi_res": noise(NOISE_HIRES, seed, 32, 32, 32, 4),
+            "curl": noise(NOISE_CURL2D, seed, 128, 128, 1, 2)[0], "weather": noise(NOISE_WEATHER, seed, 512, 512, 1, 4)[0]}
 
 
 def march(uniforms, textures, width, height, precision=32, pixel_mode=0, coverage_offset=0.0, ref_uv_1080p=0,

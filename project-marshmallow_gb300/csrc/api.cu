@@ -314,6 +314,48 @@ int mm_texture_set_format(mm_texture t, int format, void* stream) {
     return build_hw_copy(t, format, (cudaStream_t)stream);
 }
 
+}  // extern "C"
+
+namespace {
+
+// One filtered fetch of the texture's hardware copy per coordinate: (u, v) pairs for a 2D texture,
+// (u, v, w) triples for a 3D one; four floats out per fetch.
+__global__ void texture_sample_kernel(cudaTextureObject_t tex, int dims, int channels, const float* coords, size_t n,
+                                      float4* out) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 r;
+    if (dims == 3) {
+        r = tex3D<float4>(tex, coords[3 * i], coords[3 * i + 1], coords[3 * i + 2]);
+    } else if (channels == 2) {
+        const float2 q = tex2D<float2>(tex, coords[2 * i], coords[2 * i + 1]);
+        r = make_float4(q.x, q.y, 0.0f, 1.0f);
+    } else if (channels == 1) {
+        r = make_float4(tex2D<float>(tex, coords[2 * i], coords[2 * i + 1]), 0.0f, 0.0f, 1.0f);
+    } else {
+        r = tex2D<float4>(tex, coords[2 * i], coords[2 * i + 1]);
+    }
+    out[i] = r;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mm_texture_sample(mm_texture t, const float* d_coords, size_t n, float* d_out, void* stream) {
+    if (!t || (n && (!d_coords || !d_out))) return fail(MM_ERR_INVALID_ARGUMENT, "texture sample: null pointer");
+    if (n == 0) return MM_OK;
+    if (n > ((size_t)1 << 30)) return fail(MM_ERR_INVALID_ARGUMENT, "texture sample: too many coordinates");
+    const int dims = t->depth > 1 ? 3 : 2;
+    const int threads = 256;
+    texture_sample_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, (cudaStream_t)stream>>>(
+        t->tex, dims, t->channels, d_coords, n, reinterpret_cast<float4*>(d_out));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return mm::cuda_fail(e, "texture_sample_kernel launch");
+    mm::count_launch();
+    return MM_OK;
+}
+
 int mm_texture_destroy(mm_texture t) {
     if (!t) return fail(MM_ERR_INVALID_ARGUMENT, "texture: null handle");
     release(t);

@@ -117,6 +117,7 @@ SIGNATURES = {
     "mm_texture_info": (C.c_int, [C.c_void_p] + [C.POINTER(C.c_int)] * 5),
     "mm_texture_copy_to_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "mm_texture_set_format": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "mm_texture_sample": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]),
     "mm_texture_destroy": (C.c_int, [C.c_void_p]),
     "mm_march_options_default": (C.c_int, [C.POINTER(MarchOptions)]),
     "mm_context_create": (C.c_int, [C.POINTER(C.c_void_p)]),

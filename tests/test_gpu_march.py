@@ -263,3 +263,112 @@ def test_march_rejects_bad_arguments(cuda, mmlib, renderer, gpu_textures):
     u.sun.color[3] = 16.0
     assert mmlib.mm_clouds_march(renderer.ctx, C.byref(u), C.byref(st), C.byref(img), C.byref(o), None) == 1
     cuda.cuda.synchronize()
+
+
+# ------------------------------------------------------------------------------ hardware filtering
+#
+# The production march reads its textures through the texture unit, whose LINEAR filter uses 8-bit
+# fixed-point weights.  The oracle run with the same filter (oracle_frame.filter = 1, pinned fetch
+# by fetch against the hardware in test_gpu_sampler.py) is the FP32 march the GPU computes:
+#  - exact arithmetic + texture units equals it bit for bit (colour, depth, work counters);
+#  - production arithmetic (FMA contraction, SFU square roots, algebraically equal forms) against it:
+#    RMSE <= 1/255 as stated; colour within 4/255 and depth within 1e-3 relative on every pixel
+#    except those where one of the shader's hard thresholds (density > 0 at :426, < 1e-4 at
+#    :243/:437, accumulated > 0.99 at :476) falls the other way.  Such a pixel takes a different
+#    path, and the reference's own FP32 arithmetic has the same kind of pixel against FP64: the FP32
+#    oracle against the FP64 oracle, both with the texture unit's filter, on the same pixels.  The
+#    gate is that production's tail against FP32 is no larger than FP32's own tail against FP64
+#    (summed over the frames of a test), and at most 1e-4 of the pixels of any frame.
+
+
+def _tail(e):
+    return e["frac_over_4"], e["depth_frac_over_1e3"] + e["depth_finite_mismatch"]
+
+
+def _tail_gates(errs_prod, errs_ref):
+    """errs_prod: production vs FP32-TU oracle; errs_ref: FP32-TU vs FP64-TU oracle; per frame."""
+    for e in errs_prod:
+        assert e["nan"] == 0
+        assert e["rmse_255"] <= 1.0, e
+        assert e["frac_over_4"] <= 1e-4, e
+    pc = sum(_tail(e)[0] for e in errs_prod)
+    pd = sum(_tail(e)[1] for e in errs_prod)
+    rc = sum(_tail(e)[0] for e in errs_ref)
+    rd = sum(_tail(e)[1] for e in errs_ref)
+    print("colour tail (pixels > 4/255): production vs FP32 %.2e, FP32 vs FP64 %.2e; depth tail (> 1e-3): "
+          "production vs FP32 %.2e, FP32 vs FP64 %.2e (sums of per-frame fractions)" % (pc, rc, pd, rd))
+    assert pc <= rc, (pc, rc)
+    assert pd <= rd, (pd, rd)
+
+
+@pytest.mark.parametrize("frame", [0, 7, 15])
+def test_exact_hardware_bit_exact_vs_oracle_texture_unit(cuda, orc, renderer, gpu_textures, host_textures, frame):
+    # Exact arithmetic with the texture units equals the FP32 oracle with the texture unit's filter.
+    import marshmallow as mm
+    import marshmallow.lib as L
+    u = mm.scene.sweep_uniforms(frame, 1920, 1080)
+    rgba, dep = render(cuda, renderer, u, gpu_textures, 1920, 1080, sampler=L.SAMPLER_HARDWARE, math=L.MATH_EXACT)
+    ref, rdep, _ = orc.march(u, host_textures, 1920, 1080, precision=32, rows=(frame, 1080, 24),
+                             filter=orc.FILTER_TEXTURE_UNIT)
+    assert np.array_equal(rgba[frame::24].view(np.uint32), ref.view(np.uint32))
+    assert np.array_equal(dep[frame::24].view(np.uint32), rdep.view(np.uint32))
+
+
+def test_exact_hardware_counters_vs_oracle_texture_unit_256(cuda, orc, renderer, gpu_textures, host_textures):
+    import marshmallow as mm
+    import marshmallow.lib as L
+    u = mm.scene.uniforms(256, 256)
+    rgba, dep, cnt = render_counted(cuda, renderer, u, gpu_textures, 256, 256, sampler=L.SAMPLER_HARDWARE,
+                                    math=L.MATH_EXACT)
+    ref, rdep, rcnt = orc.march(u, host_textures, 256, 256, precision=32, filter=orc.FILTER_TEXTURE_UNIT)
+    assert np.array_equal(rgba.view(np.uint32), ref.view(np.uint32))
+    assert np.array_equal(dep.view(np.uint32), rdep.view(np.uint32))
+    assert np.array_equal(cnt, rcnt)
+
+
+def _prod_and_ref_errors(cuda, orc, renderer, gpu_textures, host_textures, u, w, h, r0, step, **opts):
+    import marshmallow as mm
+    rgba, dep = render(cuda, renderer, u, gpu_textures, w, h, **opts)
+    off = opts.get("coverage_offset", 0.0)
+    kw = dict(coverage_offset=off, rows=(r0, h, step), col_begin=r0, col_step=step, filter=orc.FILTER_TEXTURE_UNIT)
+    f32, d32, _ = orc.march(u, host_textures, w, h, precision=32, **kw)
+    f64, d64, _ = orc.march(u, host_textures, w, h, precision=64, **kw)
+    ep = mm.metrics.frame_errors(rgba[r0::step, r0::step], f32, dep[r0::step, r0::step], d32)
+    er = mm.metrics.frame_errors(f32, f64, d32, d64)
+    return ep, er
+
+
+def test_production_vs_oracle_texture_unit_1080p_sweep(cuda, orc, renderer, gpu_textures, host_textures):
+    # The benchmark's configuration (fast arithmetic, texture units) over the whole 16-frame sweep,
+    # every 2nd row and column.
+    import marshmallow as mm
+    prod, ref = [], []
+    for frame in range(16):
+        u = mm.scene.sweep_uniforms(frame, 1920, 1080)
+        ep, er = _prod_and_ref_errors(cuda, orc, renderer, gpu_textures, host_textures, u, 1920, 1080, frame % 2, 2)
+        prod.append(ep)
+        ref.append(er)
+        print("frame %2d production vs FP32: rmse %.3f max %.2f >4: %.1e depth>1e-3 %.1e | FP32 vs FP64: rmse %.3f "
+              "max %.2f >4: %.1e depth>1e-3 %.1e" % (frame, ep["rmse_255"], ep["max_255"], ep["frac_over_4"],
+                                                     ep["depth_frac_over_1e3"], er["rmse_255"], er["max_255"],
+                                                     er["frac_over_4"], er["depth_frac_over_1e3"]))
+    _tail_gates(prod, ref)
+
+
+def test_production_vs_oracle_texture_unit_4k_sun_coverage_sweep(cuda, orc, renderer, gpu_textures, host_textures):
+    # 3840x2160, sun elevation {5, 30, 60, 85} x coverage offset {-0.2, 0, +0.2}, every 8th row and column.
+    import marshmallow as mm
+    prod, ref = [], []
+    for el in (5.0, 30.0, 60.0, 85.0):
+        for off in (-0.2, 0.0, 0.2):
+            p = mm.scene.sweep_params(0)
+            u = mm.scene.uniforms(3840, 2160, yaw=p["yaw"], pitch=p["pitch"], time=p["time"], sun_elevation=el)
+            ep, er = _prod_and_ref_errors(cuda, orc, renderer, gpu_textures, host_textures, u, 3840, 2160, 3, 8,
+                                          coverage_offset=off)
+            prod.append(ep)
+            ref.append(er)
+            print("sun %4.1f cov %+.1f production vs FP32: rmse %.3f max %.2f >4: %.1e depth>1e-3 %.1e | FP32 vs "
+                  "FP64: rmse %.3f max %.2f >4: %.1e depth>1e-3 %.1e"
+                  % (el, off, ep["rmse_255"], ep["max_255"], ep["frac_over_4"], ep["depth_frac_over_1e3"],
+                     er["rmse_255"], er["max_255"], er["frac_over_4"], er["depth_frac_over_1e3"]))
+    _tail_gates(prod, ref)

@@ -62,9 +62,11 @@ def test_texture_unit_equals_oracle_filter(cuda, mmlib, orc, name):
         tex.close()
 
 
-@pytest.mark.parametrize("shape", [(64, 128, 4), (128, 32, 2), (16, 16, 16, 4), (8, 64, 32, 4)])
+@pytest.mark.parametrize("shape", [(64, 128, 4), (128, 32, 2), (37, 53, 4), (60, 100, 1), (16, 16, 16, 4),
+                                   (8, 64, 32, 4), (28, 20, 24, 4)])
 def test_texture_unit_equals_oracle_filter_random_texels(cuda, mmlib, orc, shape):
-    # Random bytes in textures of other power-of-two shapes and channel counts.
+    # Random bytes in textures of other shapes (sides that are not powers of two included) and
+    # channel counts.
     import marshmallow as mm
     rng = np.random.default_rng(11)
     texels = rng.integers(0, 256, shape, dtype=np.uint8)

@@ -427,8 +427,9 @@ def reference_frame_1080p(renderer, textures, flush, stream, frames=16):
 
 def train_surrogate(lib, stream):
     """The learned sun-cone surrogate as the library trains it: 2^22 samples of the plain six-tap cone
-    (texture seeds 1-8, sun 0-90 deg) by mm_surrogate_generate, then 2048 Adam steps of batch 16384
-    by mm_mlp_train on the tensor cores.  Returns the network and the training cost."""
+    (texture seeds 1-8, sun 0-90 deg) by mm_surrogate_generate, then 256 Adam steps of batch 131072
+    (8 passes over the samples) by mm_mlp_train on the tensor cores.  Returns the network and the
+    training cost."""
     import torch
     import marshmallow.lib as L
     sp = C.c_void_p(stream.cuda_stream)
@@ -445,14 +446,19 @@ def train_surrogate(lib, stream):
     net = C.c_void_p()
     L.check(lib.mm_mlp_create(11, C.byref(net)), "mm_mlp_create")
     steps = 0
-    for lr, k in ((3e-3, 1024), (1e-3, 1024)):
-        L.check(lib.mm_mlp_train(net, C.c_void_p(x.data_ptr()), C.c_void_p(t.data_ptr()), n.value, 16384, k, lr, None,
+    for lr, k in ((8e-3, 128), (2.5e-3, 128)):
+        L.check(lib.mm_mlp_train(net, C.c_void_p(x.data_ptr()), C.c_void_p(t.data_ptr()), n.value, 131072, k, lr, None,
                                  sp), "mm_mlp_train")
         steps += k
     torch.cuda.synchronize()
     t2 = time.perf_counter()
-    return net, {"samples": n.value, "generate_ms": round(1e3 * (t1 - t0), 2), "train_steps": steps, "batch": 16384,
-                 "train_ms": round(1e3 * (t2 - t1), 2),
+    # forward + backward of the 16-64-64-64-1 network: 3 x 2 x 9280 multiply-adds' FLOP per sample
+    tflops = 3 * 2 * 9280 * 131072 * steps / (t2 - t1) / 1e12
+    peaks_file = os.path.join(REPO, "MEASURED_PEAKS.json")
+    bf16 = json.load(open(peaks_file)).get("bf16_tflops") if os.path.exists(peaks_file) else None
+    return net, {"samples": n.value, "generate_ms": round(1e3 * (t1 - t0), 2), "train_steps": steps, "batch": 131072,
+                 "train_ms": round(1e3 * (t2 - t1), 2), "train_tflops": round(tflops, 1),
+                 "train_frac_of_measured_bf16": round(tflops / bf16, 4) if bf16 else None,
                  "note": "one-off cost per texture set, not part of a frame"}
 
 

@@ -508,6 +508,14 @@ int mm_measure_peaks(mm_texture tex3d, mm_texture tex2d, double* out, void* stre
 int mm_tc_gemm_check(const void* d_a, const void* d_b, int K, int N, int variant, float* d_out, int* d_status,
                      void* stream);
 
+/* The same GEMM with A and/or B read MN-major from shared memory (the in-place transposed operands
+ * of the training kernel's weight-gradient and delta GEMMs): d_a holds A^T ([K][128] row-major)
+ * when a_mn, d_b holds B^T ([K][N]) when b_mn.  lbo_k = 1 puts the stride between K groups of an
+ * MN-major operand in the descriptor's leading-byte-offset field, 0 in its stride field (the
+ * kernels use 1).  No reference counterpart. */
+int mm_tc_gemm_mn_check(const void* d_a, const void* d_b, int K, int N, int a_mn, int b_mn, int lbo_k, float* d_out,
+                        int* d_status, void* stream);
+
 /* Self-test of the bounded mbarrier wait every tensor-core kernel uses: one thread initializes an
  * mbarrier, arrives on it (arrive != 0) or not, and waits for its phase for at most poll_limit polls
  * (1 .. 2^24).  *d_status becomes 0 if the phase completed and 1 if the wait gave up — the path a

@@ -18,8 +18,9 @@
 //   d2  = bf16((d3 W3b) * [z2 > 0])                      (A = d3,   B = W3b^T)
 //   dW2 = d2^T h1, db2 = d2^T 1; d1 = bf16((d2 W2b) * [z1 > 0]); dW1 = d1^T x, db1 = d1^T 1.
 // Weight-gradient GEMMs reduce over the 128 samples (K = 128) with M padded from 64 to 128 rows;
-// the ones row appended to B yields the bias gradient as one more output column.  Each CTA adds
-// its tile's gradients to a global FP32 buffer with atomics.
+// the ones row appended to B yields the bias gradient as one more output column.  Each layer's
+// weight gradient accumulates in its own tensor-memory columns over all the tiles a CTA trains on,
+// and the CTA adds it to a global FP32 buffer with atomics once, at its end.
 //
 // The file also holds the tensor-core GEMM self-check used to validate the operand layout and the
 // MMA/TMEM protocol of tc.cuh on the device.
@@ -90,6 +91,78 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(const __nv_bfloat16* __res
     if (warp == 0) tc::tmem_dealloc(taddr, ncols);
 }
 
+// MN-major operand self-check: D[128 x N] = A[128 x K] * B[N x K]^T with A supplied as A^T ([K][128]
+// row-major) when a_mn and B as B^T ([K][N]) when b_mn; each is staged as a [K][MN] tile in the
+// K-major layout and read MN-major.  lbo_k selects which descriptor field carries the stride
+// between K groups of an MN-major operand (1: the leading-byte-offset field, 0: the stride field).
+// The operands sit 64 KB apart in a 192 KB buffer, so either reading stays inside it.
+__global__ void __launch_bounds__(128) tc_gemm_mn_kernel(const __nv_bfloat16* __restrict__ A,
+                                                         const __nv_bfloat16* __restrict__ B, int K, int N, int a_mn,
+                                                         int b_mn, int lbo_k, float* __restrict__ D, int* status) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tslot;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    uint8_t* sA = smem;
+    uint8_t* sB = smem + 65536;
+    for (int i = tid; i < 128 * K; i += 128) {
+        if (a_mn)
+            *reinterpret_cast<__nv_bfloat16*>(sA + tc::kmajor_offset(i / 128, i % 128, 128)) = A[i];  // A^T[k][m]
+        else
+            *reinterpret_cast<__nv_bfloat16*>(sA + tc::kmajor_offset(i / K, i % K, K)) = A[i];
+    }
+    for (int i = tid; i < N * K; i += 128) {
+        if (b_mn)
+            *reinterpret_cast<__nv_bfloat16*>(sB + tc::kmajor_offset(i / N, i % N, N)) = B[i];  // B^T[k][n]
+        else
+            *reinterpret_cast<__nv_bfloat16*>(sB + tc::kmajor_offset(i / K, i % K, K)) = B[i];
+    }
+    const uint32_t ncols = N <= 32 ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256));
+    if (tid == 0) tc::mbar_init(&bar, 1);
+    if (warp == 0) tc::tmem_alloc(&tslot, ncols);
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t taddr = tslot;
+    if (tid == 0) {
+        const uint32_t idesc = tc::idesc_bf16_mn(128, N, a_mn != 0, b_mn != 0);
+        for (int kk = 0; kk < K / 16; ++kk) {
+            uint64_t ad, bd;
+            if (a_mn) {
+                const uint32_t kstride = (128 / 8) * 128;
+                ad = tc::smem_desc(tc::smem_u32(sA) + kk * 2 * kstride, lbo_k ? kstride : 128u, lbo_k ? 128u : kstride);
+            } else {
+                ad = tc::smem_desc(tc::smem_u32(sA) + kk * 256, 128, (uint32_t)(K / 8) * 128);
+            }
+            if (b_mn) {
+                const uint32_t kstride = (uint32_t)(N / 8) * 128;
+                bd = tc::smem_desc(tc::smem_u32(sB) + kk * 2 * kstride, lbo_k ? kstride : 128u, lbo_k ? 128u : kstride);
+            } else {
+                bd = tc::smem_desc(tc::smem_u32(sB) + kk * 256, 128, (uint32_t)(K / 8) * 128);
+            }
+            tc::mma_bf16(taddr, ad, bd, idesc, kk > 0 ? 1u : 0u);
+        }
+        tc::mma_commit(&bar);
+    }
+    const bool ok = tc::mbar_wait(&bar, 0);
+    tc::fence_after_sync();
+    if (ok) {
+        const int row = warp * 32 + lane;
+        for (int c0 = 0; c0 < N; c0 += 16) {
+            float v[16];
+            tc::tmem_ld16(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) D[row * N + c0 + i] = v[i];
+        }
+    } else if (lane == 0) {
+        atomicExch(status, 1);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(taddr, ncols);
+}
+
 // ------------------------------------------------------------------------------ parameters
 
 // FP32 parameter vector layout.
@@ -111,11 +184,15 @@ struct SmemWeights {
 };
 
 __device__ void load_weights(SmemWeights& sw, const float* __restrict__ P, const __nv_bfloat16* __restrict__ WB) {
-    for (int i = threadIdx.x; i < kHid * kIn; i += blockDim.x)
-        *reinterpret_cast<__nv_bfloat16*>(sw.w1 + tc::kmajor_offset(i / kIn, i % kIn, kIn)) = WB[OFFB_W1 + i];
-    for (int i = threadIdx.x; i < kHid * kHid; i += blockDim.x) {
-        *reinterpret_cast<__nv_bfloat16*>(sw.w2 + tc::kmajor_offset(i / kHid, i % kHid, kHid)) = WB[OFFB_W2 + i];
-        *reinterpret_cast<__nv_bfloat16*>(sw.w3 + tc::kmajor_offset(i / kHid, i % kHid, kHid)) = WB[OFFB_W3 + i];
+    // 8 consecutive inputs of one output row are one 16-byte core-matrix row: one vector copy each.
+    const uint4* wb = reinterpret_cast<const uint4*>(WB);
+    for (int i = threadIdx.x; i < kHid * kIn / 8; i += blockDim.x)
+        *reinterpret_cast<uint4*>(sw.w1 + tc::kmajor_offset(i / (kIn / 8), (i % (kIn / 8)) * 8, kIn)) =
+            __ldg(wb + OFFB_W1 / 8 + i);
+    for (int i = threadIdx.x; i < kHid * kHid / 8; i += blockDim.x) {
+        const int o = i / (kHid / 8), k = (i % (kHid / 8)) * 8;
+        *reinterpret_cast<uint4*>(sw.w2 + tc::kmajor_offset(o, k, kHid)) = __ldg(wb + OFFB_W2 / 8 + i);
+        *reinterpret_cast<uint4*>(sw.w3 + tc::kmajor_offset(o, k, kHid)) = __ldg(wb + OFFB_W3 / 8 + i);
     }
     for (int i = threadIdx.x; i < kHid; i += blockDim.x) {
         sw.b1[i] = P[OFF_B1 + i];
@@ -124,42 +201,6 @@ __device__ void load_weights(SmemWeights& sw, const float* __restrict__ P, const
         sw.w4[i] = P[OFF_W4 + i];
     }
     if (threadIdx.x == 0) sw.b4 = P[OFF_B4];
-}
-
-// Loads the 16 bf16 features of sample `row` (zeros past n) into the calling thread's row of a
-// 128 x 16 K-major tile.
-__device__ __forceinline__ void load_x_row(uint8_t* sx, const __nv_bfloat16* __restrict__ X, int row, int n, int r) {
-    uint4 a = make_uint4(0, 0, 0, 0), b = a;
-    if (row < n) {
-        const uint4* src = reinterpret_cast<const uint4*>(X + (size_t)row * kIn);
-        a = src[0];
-        b = src[1];
-    }
-    *reinterpret_cast<uint4*>(sx + tc::kmajor_offset(r, 0, kIn)) = a;
-    *reinterpret_cast<uint4*>(sx + tc::kmajor_offset(r, 8, kIn)) = b;
-}
-
-// Epilogue of a hidden layer: 64 accumulator columns of this thread's TMEM lane + bias, ReLU.
-__device__ __forceinline__ void epilogue_relu(uint32_t t_row, const float* bias, float* h) {
-#pragma unroll
-    for (int c = 0; c < kHid; c += 16) {
-        tc::tmem_ld16(t_row + c, h + c);
-#pragma unroll
-        for (int j = 0; j < 16; ++j) h[c + j] = fmaxf(h[c + j] + bias[c + j], 0.0f);
-    }
-}
-
-// Stores 64 activations of row r as bf16 into a 128 x 64 K-major tile.
-__device__ __forceinline__ void store_row64(uint8_t* s, int r, const float* h) {
-#pragma unroll
-    for (int c = 0; c < kHid; c += 8) *reinterpret_cast<uint4*>(s + tc::kmajor_offset(r, c, kHid)) = tc::pack8_bf16(h + c);
-}
-
-// Stores 64 values of row r transposed (element [c][r]) as bf16 into an R x 128 K-major tile.
-__device__ __forceinline__ void store_col64(uint8_t* s, int r, const float* h) {
-#pragma unroll
-    for (int c = 0; c < kHid; ++c)
-        *reinterpret_cast<__nv_bfloat16*>(s + tc::kmajor_offset(c, r, 128)) = __float2bfloat16_rn(h[c]);
 }
 
 // ------------------------------------------------------------------------------ inference
@@ -172,10 +213,61 @@ struct InferSmem {
     uint32_t tslot;
 };
 
-__global__ void __launch_bounds__(128, 4) infer_kernel(const __nv_bfloat16* __restrict__ X, int n,
+// Where the prediction goes: Y[row] (forward), or folded into its ray's transmittance (the
+// surrogate march's deferred cone terms): with meta[row] = (ray, g) and ray_b[ray] = (l_n, mix),
+// beers = mix(y, max(y, 0.7 y^(1/4)), mix) (compute-clouds.comp:456-460 with exp(-dal) = y) and
+// ray_u[ray].x += beers * exp(g + l_n).
+struct InferOut {
+    float* y;
+    const float2* meta;
+    const float2* ray_b;
+    float4* ray_u;
+};
+
+__device__ __forceinline__ void load_x_regs(const __nv_bfloat16* __restrict__ X, int row, int n, uint4& a, uint4& b) {
+    a = make_uint4(0, 0, 0, 0);
+    b = a;
+    if (row < n) {
+        const uint4* src = reinterpret_cast<const uint4*>(X + (size_t)row * kIn);
+        a = __ldcs(src);
+        b = __ldcs(src + 1);
+    }
+}
+
+// Hidden-layer epilogue of this thread's TMEM lane, 16 columns at a time: + bias, ReLU, bf16 into
+// row r of the next layer's A tile.
+__device__ __forceinline__ void epilogue_hidden(uint32_t t_row, const float* bias, uint8_t* s, int r) {
+#pragma unroll
+    for (int c = 0; c < kHid; c += 16) {
+        float v[16];
+        tc::tmem_ld16(t_row + c, v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = fmaxf(v[j] + bias[c + j], 0.0f);
+        *reinterpret_cast<uint4*>(s + tc::kmajor_offset(r, c, kHid)) = tc::pack8_bf16(v);
+        *reinterpret_cast<uint4*>(s + tc::kmajor_offset(r, c + 8, kHid)) = tc::pack8_bf16(v + 8);
+    }
+}
+
+// Last layer: z = b4 + sum_j relu(z3_j + b3_j) w4_j, summed in column order.
+__device__ __forceinline__ float epilogue_out(uint32_t t_row, const SmemWeights& w) {
+    float z = w.b4;
+#pragma unroll
+    for (int c = 0; c < kHid; c += 16) {
+        float v[16];
+        tc::tmem_ld16(t_row + c, v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) z += fmaxf(v[j] + w.b3[c + j], 0.0f) * w.w4[c + j];
+    }
+    return z;
+}
+
+// One CTA of 4 warps per 128-sample tile, persistent over tiles.  The features of the CTA's next
+// tile are loaded into registers while the current tile's three GEMMs and epilogues run.
+template <bool kAccumulate>
+__global__ void __launch_bounds__(128, 5) infer_kernel(const __nv_bfloat16* __restrict__ X, int n,
                                                        const unsigned int* __restrict__ n_dev,
                                                        const float* __restrict__ P, const __nv_bfloat16* __restrict__ WB,
-                                                       float* __restrict__ Y, int* status) {
+                                                       InferOut out, int* status) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
     if (n_dev) n = min(n, (int)*n_dev);  // sample count written by an earlier kernel
@@ -191,11 +283,25 @@ __global__ void __launch_bounds__(128, 4) infer_kernel(const __nv_bfloat16* __re
     const uint32_t sx = tc::smem_u32(S.x), sh = tc::smem_u32(S.h);
     uint32_t phase = 0;
     bool failed = false;
-    float h[kHid];
+    uint4 xa, xb;
+    load_x_regs(X, (int)blockIdx.x * 128 + tid, n, xa, xb);
+    // Accumulating epilogue: the record's (ray, g) and its ray's (l_n, mix) are loaded one tile
+    // ahead as well, so the epilogue's only memory operation is a fire-and-forget atomic add.
+    float2 meta_next = make_float2(0.0f, 0.0f), rb_next = make_float2(0.0f, 0.0f);
+    if (kAccumulate && (int)blockIdx.x * 128 + tid < n) {
+        meta_next = __ldcs(out.meta + (int)blockIdx.x * 128 + tid);
+        rb_next = out.ray_b[__float_as_int(meta_next.x)];
+    }
     for (int tile = blockIdx.x; tile * 128 < n && !failed; tile += gridDim.x) {
         const int row = tile * 128 + tid;
-        load_x_row(S.x, X, row, n, tid);
+        *reinterpret_cast<uint4*>(S.x + tc::kmajor_offset(tid, 0, kIn)) = xa;
+        *reinterpret_cast<uint4*>(S.x + tc::kmajor_offset(tid, 8, kIn)) = xb;
+        const int next = (tile + (int)gridDim.x) * 128 + tid;
+        load_x_regs(X, next, n, xa, xb);
+        const float2 meta = meta_next, rb = rb_next;
+        if (kAccumulate && next < n) meta_next = __ldcs(out.meta + next);
         for (int layer = 0; layer < 3; ++layer) {
+            if (kAccumulate && layer == 1 && next < n) rb_next = out.ray_b[__float_as_int(meta_next.x)];
             tc::fence_async_smem();
             tc::fence_before_sync();
             __syncthreads();
@@ -213,14 +319,19 @@ __global__ void __launch_bounds__(128, 4) infer_kernel(const __nv_bfloat16* __re
                 break;
             }
             tc::fence_after_sync();
-            epilogue_relu(t_row, layer == 0 ? S.w.b1 : (layer == 1 ? S.w.b2 : S.w.b3), h);
-            if (layer < 2) store_row64(S.h, tid, h);
+            if (layer < 2) epilogue_hidden(t_row, layer == 0 ? S.w.b1 : S.w.b2, S.h, tid);
         }
         if (failed) break;
-        float z = S.w.b4;
-#pragma unroll
-        for (int j = 0; j < kHid; ++j) z += h[j] * S.w.w4[j];
-        if (row < n) Y[row] = 1.0f / (1.0f + __expf(-z));
+        const float z = epilogue_out(t_row, S.w);
+        if (row < n) {
+            const float y = 1.0f / (1.0f + __expf(-z));
+            if (kAccumulate) {
+                const float beers = y * (1.0f - rb.y) + fmaxf(y, 0.7f * sqrtf(sqrtf(y))) * rb.y;
+                atomicAdd(&out.ray_u[__float_as_int(meta.x)].x, beers * __expf(meta.y + rb.x));
+            } else {
+                out.y[row] = y;
+            }
+        }
     }
     if (failed && tid == 0) atomicExch(status, 1);
     tc::fence_before_sync();
@@ -229,19 +340,28 @@ __global__ void __launch_bounds__(128, 4) infer_kernel(const __nv_bfloat16* __re
 }
 
 // ------------------------------------------------------------------------------ training
+//
+// Shared-memory tiles, all in the K-major layout of tc.cuh, each also read MN-major (transposed in
+// place) by the weight-gradient GEMMs:
+//   x  [128][32]:  features in columns 0..15, a ones column 16, zeros 17..31
+//   h1 [128][80], h2 [128][80]: activations in 0..63, ones column 64, zeros 65..79
+//   d  [128][128]: the delta of the current layer in 0..63, zeros 64..127
+// GEMMs per tile (D in TMEM, A x B^T):
+//   forward       z1 = x W1^T      A = x (K-major, K = 16)    B = W1 (K-major)
+//                 z2 = h1 W2^T, z3 = h2 W3^T
+//   weight grads  dW3|db3 += d3^T [h2 1]   A = d (MN-major, M = 128 rows of which 64 real, K = 128 samples)
+//                                          B = h2 (MN-major, N = 80)
+//                 dW2|db2 += d2^T [h1 1],  dW1|db1 += d1^T [x 1] (N = 32)
+//   deltas        d2 = (d3 W3) * [z2 > 0]  A = d (K-major, K = 64), B = W3 (MN-major: [out][in] read as [in][out])
+//                 d1 = (d2 W2) * [z1 > 0]
+// The ones columns turn the bias gradients into one more output column of the weight-gradient GEMMs.
 
 struct TrainSmem {
     SmemWeights w;
-    alignas(128) uint8_t w2t[kHid * kHid * 2];    // B of d1 = d2 W2b: [in][out]
-    alignas(128) uint8_t w3t[kHid * kHid * 2];    // B of d2 = d3 W3b
-    alignas(128) uint8_t x[128 * kIn * 2];        // A of layer 1
-    alignas(128) uint8_t xt[32 * 128 * 2];        // B of dW1: rows 0..15 x^T, row 16 ones, rest zero
-    alignas(128) uint8_t h1[128 * kHid * 2];      // A of layer 2 (and ReLU mask of layer 1)
-    alignas(128) uint8_t h2[128 * kHid * 2];      // A of layer 3 (and ReLU mask of layer 2)
-    alignas(128) uint8_t h1t[80 * 128 * 2];       // B of dW2: rows 0..63 h1^T, row 64 ones, rest zero
-    alignas(128) uint8_t h2t[80 * 128 * 2];       // B of dW3
-    alignas(128) uint8_t d[128 * kHid * 2];       // A of the d_{l-1} GEMM
-    alignas(128) uint8_t dt[128 * 128 * 2];       // A of dW: rows 0..63 d^T, rows 64..127 zero
+    alignas(128) uint8_t x[128 * 32 * 2];
+    alignas(128) uint8_t h1[128 * 80 * 2];
+    alignas(128) uint8_t h2[128 * 80 * 2];
+    alignas(128) uint8_t d[128 * 128 * 2];
     uint64_t bar;
     uint32_t tslot;
 };
@@ -252,9 +372,9 @@ __device__ __forceinline__ float warp_sum(float v) {
     return v;
 }
 
-// Adds the weight gradient tile of layer l (TMEM columns [col, col + n_in] of lanes 0..63, the
-// last one the bias) to the global gradient buffer.  Run by warps 0 and 1.
-__device__ __forceinline__ void flush_dw(uint32_t t_row, int o, int n_in, float* G, int off_w, int off_b) {
+// Writes a weight-gradient tile (TMEM columns [0, n_in] of lanes 0..63 from t_row, the last one the
+// bias) into the CTA's row of partial gradients.  Run by warps 0 and 1.
+__device__ __forceinline__ void flush_dw(uint32_t t_row, int o, int n_in, float* Gp, int off_w, int off_b) {
     float v[16];
     for (int c = 0; c < n_in + 16; c += 16) {
         tc::tmem_ld16(t_row + c, v);
@@ -262,47 +382,114 @@ __device__ __forceinline__ void flush_dw(uint32_t t_row, int o, int n_in, float*
         for (int j = 0; j < 16; ++j) {
             const int i = c + j;
             if (i < n_in)
-                atomicAdd(G + off_w + o * n_in + i, v[j]);
+                Gp[off_w + o * n_in + i] = v[j];
             else if (i == n_in)
-                atomicAdd(G + off_b + o, v[j]);
+                Gp[off_b + o] = v[j];
         }
     }
 }
 
-// Writes row r of a delta: row layout (A of the next delta GEMM) and transposed (A of dW).
-__device__ __forceinline__ void store_delta(TrainSmem& S, int r, const float* d) {
-    store_row64(S.d, r, d);
-    store_col64(S.dt, r, d);
+// K-major x K-major GEMM where the operand tiles are wider than the K used: a_cols / b_cols are the
+// tiles' widths (their 8-row groups are (cols / 8) * 128 bytes apart).
+__device__ __forceinline__ void gemm_kk(uint32_t d_tmem, uint32_t sa, int a_cols, uint32_t sb, int b_cols, int K, int N,
+                                        uint32_t idesc, uint32_t accumulate) {
+    for (int kk = 0; kk < K / 16; ++kk)
+        tc::mma_bf16(d_tmem, tc::smem_desc(sa + kk * 256, 128, (uint32_t)(a_cols / 8) * 128),
+                     tc::smem_desc(sb + kk * 256, 128, (uint32_t)(b_cols / 8) * 128), idesc, kk > 0 ? 1u : accumulate);
 }
 
-__global__ void __launch_bounds__(128, 1) train_kernel(const __nv_bfloat16* __restrict__ X, const float* __restrict__ T,
+// Weight-gradient GEMM: A = d read MN-major (M = 128, K = 128 samples), B = an activation tile of
+// width n_cols read MN-major (N = n_cols).  MN-major operands: K groups (8 samples) are
+// (cols / 8) * 128 bytes apart (descriptor leading-byte-offset field), MN groups 128 bytes.
+__device__ __forceinline__ void gemm_dw(uint32_t d_tmem, uint32_t s_d, uint32_t s_act, int n_cols, uint32_t accumulate) {
+    const uint32_t idesc = tc::idesc_bf16_mn(128, n_cols, true, true);
+    const uint32_t ka = (128 / 8) * 128, kb = (uint32_t)(n_cols / 8) * 128;
+    for (int kk = 0; kk < 128 / 16; ++kk)
+        tc::mma_bf16(d_tmem, tc::smem_desc(s_d + kk * 2 * ka, ka, 128), tc::smem_desc(s_act + kk * 2 * kb, kb, 128), idesc,
+                     kk > 0 ? 1u : accumulate);
+}
+
+// Delta GEMM: D = d (K-major, K = 64, tile width 128) x W (the [64 out][64 in] forward weight tile
+// read MN-major as [in][out]).
+__device__ __forceinline__ void gemm_delta(uint32_t d_tmem, uint32_t s_d, uint32_t s_w) {
+    const uint32_t idesc = tc::idesc_bf16_mn(128, kHid, false, true);
+    const uint32_t kb = (kHid / 8) * 128;
+    for (int kk = 0; kk < kHid / 16; ++kk)
+        tc::mma_bf16(d_tmem, tc::smem_desc(s_d + kk * 256, 128, (128 / 8) * 128),
+                     tc::smem_desc(s_w + kk * 2 * kb, kb, 128), idesc, kk > 0 ? 1u : 0u);
+}
+
+// Features of the thread's row (zeros past n) and its target.
+__device__ __forceinline__ void load_sample(const __nv_bfloat16* __restrict__ X, const float* __restrict__ T, int row,
+                                            int n, uint4& a, uint4& b, float& t) {
+    a = make_uint4(0, 0, 0, 0);
+    b = a;
+    t = 0.0f;
+    if (row < n) {
+        const uint4* src = reinterpret_cast<const uint4*>(X + (size_t)row * kIn);
+        a = __ldg(src);
+        b = __ldg(src + 1);
+        t = __ldg(T + row);
+    }
+}
+
+// Hidden-layer epilogue into an activation tile of width 80: + bias, ReLU, bf16.
+__device__ __forceinline__ void train_epilogue_hidden(uint32_t t_row, const float* bias, uint8_t* s, int r) {
+#pragma unroll
+    for (int c = 0; c < kHid; c += 16) {
+        float v[16];
+        tc::tmem_ld16(t_row + c, v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = fmaxf(v[j] + bias[c + j], 0.0f);
+        *reinterpret_cast<uint4*>(s + tc::kmajor_offset(r, c, 80)) = tc::pack8_bf16(v);
+        *reinterpret_cast<uint4*>(s + tc::kmajor_offset(r, c + 8, 80)) = tc::pack8_bf16(v + 8);
+    }
+}
+
+// Delta epilogue: (TMEM row) * [activation of the layer below > 0] as bf16 into d.
+__device__ __forceinline__ void train_epilogue_delta(uint32_t t_row, const uint8_t* act, uint8_t* d, int r) {
+#pragma unroll
+    for (int c = 0; c < kHid; c += 16) {
+        float v[16];
+        tc::tmem_ld16(t_row + c, v);
+#pragma unroll
+        for (int j = 0; j < 16; j += 8) {
+            const uint4 m = *reinterpret_cast<const uint4*>(act + tc::kmajor_offset(r, c + j, 80));
+            const __nv_bfloat16* mb = reinterpret_cast<const __nv_bfloat16*>(&m);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) v[j + q] = __bfloat162float(mb[q]) > 0.0f ? v[j + q] : 0.0f;
+        }
+        *reinterpret_cast<uint4*>(d + tc::kmajor_offset(r, c, 128)) = tc::pack8_bf16(v);
+        *reinterpret_cast<uint4*>(d + tc::kmajor_offset(r, c + 8, 128)) = tc::pack8_bf16(v + 8);
+    }
+}
+
+// Each CTA trains on tiles tile0 + blockIdx.x, + gridDim.x, ... and writes its gradient sum (and
+// its squared-error sum at index kParams) as row blockIdx.x of Gp (kParams + 1 floats per row);
+// the rows are summed by the Adam (or gradient) kernel, so no two CTAs write the same address.
+__global__ void __launch_bounds__(128, 2) train_kernel(const __nv_bfloat16* __restrict__ X, const float* __restrict__ T,
                                                        int n, int tile0, int tiles, float inv_batch,
                                                        const float* __restrict__ P,
-                                                       const __nv_bfloat16* __restrict__ WB, float* __restrict__ G,
-                                                       float* __restrict__ loss, int* status) {
+                                                       const __nv_bfloat16* __restrict__ WB, float* __restrict__ Gp_all,
+                                                       int* status) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     TrainSmem& S = *reinterpret_cast<TrainSmem*>(smem_raw);
+    __shared__ float s_out[kHid + 2];  // w4 gradient, b4 gradient, loss of the CTA
+    float* Gp = Gp_all + (size_t)blockIdx.x * (kParams + 1);
+    if (threadIdx.x < kHid + 2) s_out[threadIdx.x] = 0.0f;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     load_weights(S.w, P, WB);
-    for (int i = tid; i < kHid * kHid; i += 128) {
-        const int o = i / kHid, in = i % kHid;
-        *reinterpret_cast<__nv_bfloat16*>(S.w2t + tc::kmajor_offset(in, o, kHid)) = WB[OFFB_W2 + i];
-        *reinterpret_cast<__nv_bfloat16*>(S.w3t + tc::kmajor_offset(in, o, kHid)) = WB[OFFB_W3 + i];
-    }
-    // Padding rows of the transposed operands: ones rows give bias gradients, the rest stay zero.
+    // Constant columns: ones (bias gradients) and zeros (padding), written once.
     {
         const __nv_bfloat16 one = __float2bfloat16_rn(1.0f), zero = __float2bfloat16_rn(0.0f);
-        for (int i = tid; i < 16 * 128; i += 128) {
-            const int rr = 16 + i / 128, k = i % 128;
-            *reinterpret_cast<__nv_bfloat16*>(S.xt + tc::kmajor_offset(rr, k, 128)) = rr == 16 ? one : zero;
+        for (int c = 16; c < 32; ++c)
+            *reinterpret_cast<__nv_bfloat16*>(S.x + tc::kmajor_offset(tid, c, 32)) = c == 16 ? one : zero;
+        for (int c = 64; c < 80; ++c) {
+            *reinterpret_cast<__nv_bfloat16*>(S.h1 + tc::kmajor_offset(tid, c, 80)) = c == 64 ? one : zero;
+            *reinterpret_cast<__nv_bfloat16*>(S.h2 + tc::kmajor_offset(tid, c, 80)) = c == 64 ? one : zero;
         }
-        for (int i = tid; i < 16 * 128; i += 128) {
-            const int rr = 64 + i / 128, k = i % 128;
-            *reinterpret_cast<__nv_bfloat16*>(S.h1t + tc::kmajor_offset(rr, k, 128)) = rr == 64 ? one : zero;
-            *reinterpret_cast<__nv_bfloat16*>(S.h2t + tc::kmajor_offset(rr, k, 128)) = rr == 64 ? one : zero;
-        }
-        for (int i = tid; i < 64 * 128; i += 128)
-            *reinterpret_cast<__nv_bfloat16*>(S.dt + tc::kmajor_offset(64 + i / 128, i % 128, 128)) = zero;
+        for (int c = 64; c < 128; c += 8)
+            *reinterpret_cast<uint4*>(S.d + tc::kmajor_offset(tid, c, 128)) = make_uint4(0, 0, 0, 0);
     }
     if (tid == 0) tc::mbar_init(&S.bar, 1);
     if (warp == 0) tc::tmem_alloc(&S.tslot, 256);
@@ -311,7 +498,12 @@ __global__ void __launch_bounds__(128, 1) train_kernel(const __nv_bfloat16* __re
     tc::fence_after_sync();
     const uint32_t taddr = S.tslot;
     const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
-    const uint32_t tA = taddr, tB = taddr + 128;  // activations / deltas; weight gradients
+    // Tensor-memory columns: activations / deltas (64), then the weight gradients of layers 3 and 2
+    // (64 + bias + padding = 80 each) and 1 (16 + bias + padding = 32), summed over the CTA's tiles.
+    const uint32_t tA = taddr, tW3 = taddr + 64, tW2 = taddr + 144, tW1 = taddr + 224;
+    const uint32_t sx = tc::smem_u32(S.x), sh1 = tc::smem_u32(S.h1), sh2 = tc::smem_u32(S.h2), sd = tc::smem_u32(S.d);
+    const uint32_t idesc_fwd = tc::idesc_bf16(128, kHid);
+    uint32_t acc_dw = 0;  // 0 for the CTA's first tile: its gradient GEMMs overwrite the columns
     uint32_t phase = 0;
     bool failed = false;
     float acc_dw4[kHid];
@@ -319,13 +511,16 @@ __global__ void __launch_bounds__(128, 1) train_kernel(const __nv_bfloat16* __re
     for (int j = 0; j < kHid; ++j) acc_dw4[j] = 0.0f;
     float acc_db4 = 0.0f, acc_loss = 0.0f;
 
-    auto sync_mma = [&]() {
+    // Issues one group of MMAs from thread 0 after the block's shared-memory writes, then waits.
+    auto run_mma = [&](auto&& issue) -> bool {
         tc::fence_async_smem();
         tc::fence_before_sync();
         __syncthreads();
         tc::fence_after_sync();
-    };
-    auto wait_mma = [&]() -> bool {
+        if (tid == 0) {
+            issue();
+            tc::mma_commit(&S.bar);
+        }
         const bool ok = tc::mbar_wait(&S.bar, phase);
         phase ^= 1u;
         if (__syncthreads_or(!ok)) return false;
@@ -333,108 +528,98 @@ __global__ void __launch_bounds__(128, 1) train_kernel(const __nv_bfloat16* __re
         return true;
     };
 
+    uint4 xa, xb;
+    float tv;
+    load_sample(X, T, (tile0 + (int)blockIdx.x) * 128 + tid, n, xa, xb, tv);
     for (int tile = tile0 + blockIdx.x; tile < tile0 + tiles && !failed; tile += gridDim.x) {
         const int row = tile * 128 + tid;
         const bool valid = row < n;
+        const float target = tv;
+        *reinterpret_cast<uint4*>(S.x + tc::kmajor_offset(tid, 0, 32)) = xa;
+        *reinterpret_cast<uint4*>(S.x + tc::kmajor_offset(tid, 8, 32)) = xb;
+        if (tile + (int)gridDim.x < tile0 + tiles) load_sample(X, T, (tile + (int)gridDim.x) * 128 + tid, n, xa, xb, tv);
         // ---- forward
-        load_x_row(S.x, X, row, n, tid);
-        {
-            const __nv_bfloat16* xr = X + (size_t)row * kIn;
-#pragma unroll
-            for (int c = 0; c < kIn; ++c)
-                *reinterpret_cast<__nv_bfloat16*>(S.xt + tc::kmajor_offset(c, tid, 128)) =
-                    valid ? xr[c] : __float2bfloat16_rn(0.0f);
-        }
-        float h[kHid];
-        for (int layer = 0; layer < 3; ++layer) {
-            sync_mma();
-            if (tid == 0) {
-                if (layer == 0)
-                    tc::gemm_issue(tA, tc::smem_u32(S.x), tc::smem_u32(S.w.w1), kIn, kHid, &S.bar);
-                else
-                    tc::gemm_issue(tA, tc::smem_u32(layer == 1 ? S.h1 : S.h2), tc::smem_u32(layer == 1 ? S.w.w2 : S.w.w3),
-                                   kHid, kHid, &S.bar);
-            }
-            if (!wait_mma()) {
-                failed = true;
-                break;
-            }
-            epilogue_relu(tA + lane_off, layer == 0 ? S.w.b1 : (layer == 1 ? S.w.b2 : S.w.b3), h);
-            if (layer == 0) {
-                store_row64(S.h1, tid, h);
-                store_col64(S.h1t, tid, h);
-            } else if (layer == 1) {
-                store_row64(S.h2, tid, h);
-                store_col64(S.h2t, tid, h);
-            }
+        if (!(failed = !run_mma([&] { gemm_kk(tA, sx, 32, tc::smem_u32(S.w.w1), kIn, kIn, kHid, idesc_fwd, 0u); }))) {
+            train_epilogue_hidden(tA + lane_off, S.w.b1, S.h1, tid);
         }
         if (failed) break;
-        // ---- output layer and loss (CUDA cores)
+        if (!(failed = !run_mma([&] { gemm_kk(tA, sh1, 80, tc::smem_u32(S.w.w2), kHid, kHid, kHid, idesc_fwd, 0u); }))) {
+            train_epilogue_hidden(tA + lane_off, S.w.b2, S.h2, tid);
+        }
+        if (failed) break;
+        if ((failed = !run_mma([&] { gemm_kk(tA, sh2, 80, tc::smem_u32(S.w.w3), kHid, kHid, kHid, idesc_fwd, 0u); })))
+            break;
+        // ---- output layer, loss, and the output-layer delta (CUDA cores)
         float z = S.w.b4;
 #pragma unroll
-        for (int j = 0; j < kHid; ++j) z += h[j] * S.w.w4[j];
+        for (int c = 0; c < kHid; c += 16) {
+            float v[16];
+            tc::tmem_ld16(tA + lane_off + c, v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) z += fmaxf(v[j] + S.w.b3[c + j], 0.0f) * S.w.w4[c + j];
+        }
         const float y = 1.0f / (1.0f + expf(-z));
-        const float err = valid ? y - T[row] : 0.0f;
+        const float err = valid ? y - target : 0.0f;
         const float dz = 2.0f * err * y * (1.0f - y) * inv_batch;
         acc_loss += err * err;
         acc_db4 += dz;
-        float d[kHid];
 #pragma unroll
-        for (int j = 0; j < kHid; ++j) {
-            acc_dw4[j] += dz * h[j];
-            d[j] = h[j] > 0.0f ? dz * S.w.w4[j] : 0.0f;
+        for (int c = 0; c < kHid; c += 16) {
+            float v[16];
+            tc::tmem_ld16(tA + lane_off + c, v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const float h = fmaxf(v[j] + S.w.b3[c + j], 0.0f);
+                acc_dw4[c + j] += dz * h;
+                v[j] = h > 0.0f ? dz * S.w.w4[c + j] : 0.0f;
+            }
+            *reinterpret_cast<uint4*>(S.d + tc::kmajor_offset(tid, c, 128)) = tc::pack8_bf16(v);
+            *reinterpret_cast<uint4*>(S.d + tc::kmajor_offset(tid, c + 8, 128)) = tc::pack8_bf16(v + 8);
         }
-        // ---- layers 3, 2, 1
-        for (int l = 3; l >= 1 && !failed; --l) {
-            store_delta(S, tid, d);
-            sync_mma();
-            if (tid == 0) {
-                const uint32_t sdt = tc::smem_u32(S.dt);
-                if (l == 3) tc::gemm_mmas(tB, sdt, tc::smem_u32(S.h2t), 128, 80);
-                if (l == 2) tc::gemm_mmas(tB, sdt, tc::smem_u32(S.h1t), 128, 80);
-                if (l == 1) tc::gemm_mmas(tB, sdt, tc::smem_u32(S.xt), 128, 32);
-                if (l > 1) tc::gemm_mmas(tA, tc::smem_u32(S.d), tc::smem_u32(l == 3 ? S.w3t : S.w2t), kHid, kHid);
-                tc::mma_commit(&S.bar);
-            }
-            if (!wait_mma()) {
-                failed = true;
-                break;
-            }
-            if (warp < 2) {
-                const int o = warp * 32 + lane;
-                if (l == 3) flush_dw(tB + lane_off, o, kHid, G, OFF_W3, OFF_B3);
-                if (l == 2) flush_dw(tB + lane_off, o, kHid, G, OFF_W2, OFF_B2);
-                if (l == 1) flush_dw(tB + lane_off, o, kIn, G, OFF_W1, OFF_B1);
-            }
-            if (l > 1) {
-                const uint8_t* hm = l == 3 ? S.h2 : S.h1;  // ReLU mask of the layer below
-#pragma unroll
-                for (int c = 0; c < kHid; c += 16) {
-                    float v[16];
-                    tc::tmem_ld16(tA + lane_off + c, v);
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) {
-                        const float hv = __bfloat162float(
-                            *reinterpret_cast<const __nv_bfloat16*>(hm + tc::kmajor_offset(tid, c + j, kHid)));
-                        d[c + j] = hv > 0.0f ? v[j] : 0.0f;
-                    }
-                }
-            }
-            // the next iteration overwrites S.d / S.dt, which these MMAs read: they have completed
+        // ---- layer 3: dW3 and the delta of layer 2
+        if (!(failed = !run_mma([&] {
+                  gemm_dw(tW3, sd, sh2, 80, acc_dw);
+                  gemm_delta(tA, sd, tc::smem_u32(S.w.w3));
+              }))) {
+            train_epilogue_delta(tA + lane_off, S.h2, S.d, tid);
         }
+        if (failed) break;
+        // ---- layer 2: dW2 and the delta of layer 1
+        if (!(failed = !run_mma([&] {
+                  gemm_dw(tW2, sd, sh1, 80, acc_dw);
+                  gemm_delta(tA, sd, tc::smem_u32(S.w.w2));
+              }))) {
+            train_epilogue_delta(tA + lane_off, S.h1, S.d, tid);
+        }
+        if (failed) break;
+        // ---- layer 1: dW1
+        if ((failed = !run_mma([&] { gemm_dw(tW1, sd, sx, 32, acc_dw); }))) break;
+        acc_dw = 1u;
     }
-    // ---- output-layer gradients and loss
+    // ---- hidden-layer weight gradients of all the CTA's tiles
+    if (!failed && acc_dw && warp < 2) {
+        const int o = warp * 32 + lane;
+        flush_dw(tW3 + lane_off, o, kHid, Gp, OFF_W3, OFF_B3);
+        flush_dw(tW2 + lane_off, o, kHid, Gp, OFF_W2, OFF_B2);
+        flush_dw(tW1 + lane_off, o, kIn, Gp, OFF_W1, OFF_B1);
+    }
+    // ---- output-layer gradients and loss: warp sums, then the CTA's sum
+#pragma unroll
     for (int j = 0; j < kHid; ++j) {
         const float v = warp_sum(acc_dw4[j]);
-        if (lane == 0) atomicAdd(G + OFF_W4 + j, v);
+        if (lane == 0) atomicAdd(&s_out[j], v);
     }
     {
         const float v = warp_sum(acc_db4), l2 = warp_sum(acc_loss);
         if (lane == 0) {
-            atomicAdd(G + OFF_B4, v);
-            if (loss) atomicAdd(loss, l2);
+            atomicAdd(&s_out[kHid], v);
+            atomicAdd(&s_out[kHid + 1], l2);
         }
     }
+    __syncthreads();
+    if (tid < kHid) Gp[OFF_W4 + tid] = s_out[tid];
+    if (tid == kHid) Gp[OFF_B4] = s_out[kHid];
+    if (tid == kHid + 1) Gp[kParams] = s_out[kHid + 1];
     if (failed && tid == 0) atomicExch(status, 1);
     tc::fence_before_sync();
     __syncthreads();
@@ -442,19 +627,34 @@ __global__ void __launch_bounds__(128, 1) train_kernel(const __nv_bfloat16* __re
 }
 
 // Adam on the FP32 parameters; refreshes the BF16 copies and clears the gradient buffer.
-__global__ void adam_kernel(float* __restrict__ P, __nv_bfloat16* __restrict__ WB, float* __restrict__ G,
-                            float* __restrict__ Mo, float* __restrict__ Vo, float lr, float b1, float b2, float eps,
-                            float c1, float c2) {
+// Sum of the training kernel's `parts` partial rows at index i (i == kParams: the squared error).
+__device__ __forceinline__ float sum_parts(const float* __restrict__ Gp, int parts, int i) {
+    float g = 0.0f;
+    for (int c = 0; c < parts; ++c) g += Gp[(size_t)c * (kParams + 1) + i];
+    return g;
+}
+
+// Gradient (and loss) of a training launch into G and *loss, for callers that read the gradient.
+__global__ void reduce_grad_kernel(const float* __restrict__ Gp, int parts, float* __restrict__ G,
+                                   float* __restrict__ loss) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < kParams) G[i] = sum_parts(Gp, parts, i);
+    if (i == kParams && loss) *loss = sum_parts(Gp, parts, i);
+}
+
+__global__ void adam_kernel(float* __restrict__ P, __nv_bfloat16* __restrict__ WB, const float* __restrict__ Gp,
+                            int parts, float* __restrict__ loss, float* __restrict__ Mo, float* __restrict__ Vo,
+                            float lr, float b1, float b2, float eps, float c1, float c2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == kParams && loss) *loss = sum_parts(Gp, parts, i);
     if (i >= kParams) return;
-    const float g = G[i];
+    const float g = sum_parts(Gp, parts, i);
     const float m = b1 * Mo[i] + (1.0f - b1) * g;
     const float v = b2 * Vo[i] + (1.0f - b2) * g * g;
     Mo[i] = m;
     Vo[i] = v;
     const float p = P[i] - lr * (m / c1) / (sqrtf(v / c2) + eps);
     P[i] = p;
-    G[i] = 0.0f;
     if (i < OFF_B1)
         WB[OFFB_W1 + (i - OFF_W1)] = __float2bfloat16_rn(p);
     else if (i >= OFF_W2 && i < OFF_B2)
@@ -480,7 +680,7 @@ __global__ void refresh_bf16_kernel(const float* __restrict__ P, __nv_bfloat16* 
 struct mm_mlp_s {
     float* P = nullptr;          // FP32 parameters
     __nv_bfloat16* WB = nullptr;  // BF16 copies of W1..W3
-    float* G = nullptr;          // gradient accumulator (kept zero between steps)
+    float* Gp = nullptr;         // per-CTA partial gradients + squared error of a training launch
     float* M = nullptr;          // Adam first moment
     float* V = nullptr;          // Adam second moment
     float* loss = nullptr;       // one float
@@ -497,7 +697,10 @@ size_t train_smem() { return sizeof(mm::mlp::TrainSmem) + 1024; }
 int set_smem_limits() {
     static bool done = false;
     if (done) return MM_OK;
-    MM_CUDA_TRY(cudaFuncSetAttribute(mm::mlp::infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)infer_smem()));
+    MM_CUDA_TRY(cudaFuncSetAttribute(mm::mlp::infer_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)infer_smem()));
+    MM_CUDA_TRY(cudaFuncSetAttribute(mm::mlp::infer_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)infer_smem()));
     MM_CUDA_TRY(cudaFuncSetAttribute(mm::mlp::train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()));
     done = true;
     return MM_OK;
@@ -518,12 +721,15 @@ int refresh(mm_mlp m, cudaStream_t s) {
     return MM_OK;
 }
 
-// Runs the training kernel over tiles [tile0, tile0 + tiles) of (X, T) adding into m->G.
+// Partial-gradient rows of a training launch over `tiles` tiles: two CTAs per SM, each at least one tile.
+int train_grid(mm_mlp m, int tiles) { return tiles < 2 * m->num_sms ? tiles : 2 * m->num_sms; }
+
+// Runs the training kernel over tiles [tile0, tile0 + tiles) of (X, T) into m->Gp (train_grid rows).
 int run_train(mm_mlp m, const void* X, const float* T, int n, int tile0, int tiles, float inv_batch, cudaStream_t s) {
-    const int grid = tiles < m->num_sms ? tiles : m->num_sms;
+    const int grid = train_grid(m, tiles);
     // The shared-memory image needs 1024-byte alignment; the kernel takes the dynamic buffer as is.
     mm::mlp::train_kernel<<<grid, 128, train_smem(), s>>>((const __nv_bfloat16*)X, T, n, tile0, tiles, inv_batch, m->P,
-                                                         m->WB, m->G, m->loss, m->status);
+                                                         m->WB, m->Gp, m->status);
     MM_CUDA_TRY(cudaGetLastError());
     mm::count_launch();
     return MM_OK;
@@ -533,15 +739,17 @@ int run_train(mm_mlp m, const void* X, const float* T, int n, int tile0, int til
 
 namespace mm {
 
-// Inference on up to `cap` samples, the actual count read from device memory (surrogate march).
-int mlp_infer_device_count(mm_mlp m, const void* d_x, int cap, const unsigned int* d_count, float* d_y,
-                           cudaStream_t s) {
+// Inference on up to `cap` deferred cone samples of the surrogate march (the actual count read from
+// device memory), each prediction folded into its ray's transmittance (InferOut above).
+int mlp_infer_accumulate(mm_mlp m, const void* d_x, int cap, const unsigned int* d_count, const float2* meta,
+                         const float2* ray_b, float4* ray_u, cudaStream_t s) {
     int r = set_smem_limits();
     if (r) return r;
     const int tiles = (cap + 127) / 128;
-    const int grid = tiles < 4 * m->num_sms ? tiles : 4 * m->num_sms;
-    mlp::infer_kernel<<<grid, 128, infer_smem(), s>>>((const __nv_bfloat16*)d_x, cap, d_count, m->P, m->WB, d_y,
-                                                      m->status);
+    const int grid = tiles < 5 * m->num_sms ? tiles : 5 * m->num_sms;
+    mlp::InferOut o{nullptr, meta, ray_b, ray_u};
+    mlp::infer_kernel<true><<<grid, 128, infer_smem(), s>>>((const __nv_bfloat16*)d_x, cap, d_count, m->P, m->WB, o,
+                                                            m->status);
     MM_CUDA_TRY(cudaGetLastError());
     count_launch();
     return MM_OK;
@@ -568,7 +776,7 @@ int mm_mlp_create(uint32_t seed, mm_mlp* out) {
     cudaError_t e = cudaSuccess;
     e = e ? e : cudaMalloc(&m->P, kParams * sizeof(float));
     e = e ? e : cudaMalloc(&m->WB, kBf16 * sizeof(__nv_bfloat16));
-    e = e ? e : cudaMalloc(&m->G, kParams * sizeof(float));
+    e = e ? e : cudaMalloc(&m->Gp, (size_t)2 * m->num_sms * (kParams + 1) * sizeof(float));
     e = e ? e : cudaMalloc(&m->M, kParams * sizeof(float));
     e = e ? e : cudaMalloc(&m->V, kParams * sizeof(float));
     e = e ? e : cudaMalloc(&m->loss, sizeof(float));
@@ -592,7 +800,6 @@ int mm_mlp_create(uint32_t seed, mm_mlp* out) {
     for (int i = 0; i < kHid; ++i) h[OFF_W4 + i] = a2 * 0.5f * uni();
     e = cudaMemcpy(m->P, h, kParams * sizeof(float), cudaMemcpyHostToDevice);
     delete[] h;
-    e = e ? e : cudaMemset(m->G, 0, kParams * sizeof(float));
     e = e ? e : cudaMemset(m->M, 0, kParams * sizeof(float));
     e = e ? e : cudaMemset(m->V, 0, kParams * sizeof(float));
     e = e ? e : cudaMemset(m->status, 0, sizeof(int));
@@ -608,7 +815,7 @@ int mm_mlp_destroy(mm_mlp m) {
     if (!m) return mm::fail(MM_ERR_INVALID_ARGUMENT, "mlp: null handle");
     cudaFree(m->P);
     cudaFree(m->WB);
-    cudaFree(m->G);
+    cudaFree(m->Gp);
     cudaFree(m->M);
     cudaFree(m->V);
     cudaFree(m->loss);
@@ -640,9 +847,10 @@ int mm_mlp_forward(mm_mlp m, const void* d_x, int n, float* d_y, void* stream) {
     if (r) return r;
     cudaStream_t s = (cudaStream_t)stream;
     const int tiles = (n + 127) / 128;
-    const int grid = tiles < 4 * m->num_sms ? tiles : 4 * m->num_sms;
-    mm::mlp::infer_kernel<<<grid, 128, infer_smem(), s>>>((const __nv_bfloat16*)d_x, n, nullptr, m->P, m->WB, d_y,
-                                                          m->status);
+    const int grid = tiles < 5 * m->num_sms ? tiles : 5 * m->num_sms;
+    mm::mlp::InferOut o{d_y, nullptr, nullptr, nullptr};
+    mm::mlp::infer_kernel<false><<<grid, 128, infer_smem(), s>>>((const __nv_bfloat16*)d_x, n, nullptr, m->P, m->WB, o,
+                                                                 m->status);
     MM_CUDA_TRY(cudaGetLastError());
     mm::count_launch();
     return MM_OK;
@@ -654,11 +862,12 @@ int mm_mlp_gradients(mm_mlp m, const void* d_x, const float* d_t, int n, float* 
     int r = set_smem_limits();
     if (r) return r;
     cudaStream_t s = (cudaStream_t)stream;
-    MM_CUDA_TRY(cudaMemsetAsync(m->G, 0, mm::mlp::kParams * sizeof(float), s));
-    MM_CUDA_TRY(cudaMemsetAsync(m->loss, 0, sizeof(float), s));
-    if ((r = run_train(m, d_x, d_t, n, 0, (n + 127) / 128, 1.0f / (float)n, s))) return r;
-    MM_CUDA_TRY(cudaMemcpyAsync(d_grad, m->G, mm::mlp::kParams * sizeof(float), cudaMemcpyDeviceToDevice, s));
-    MM_CUDA_TRY(cudaMemsetAsync(m->G, 0, mm::mlp::kParams * sizeof(float), s));
+    const int tiles = (n + 127) / 128;
+    if ((r = run_train(m, d_x, d_t, n, 0, tiles, 1.0f / (float)n, s))) return r;
+    mm::mlp::reduce_grad_kernel<<<(mm::mlp::kParams + 256) / 256, 256, 0, s>>>(m->Gp, train_grid(m, tiles), d_grad,
+                                                                              m->loss);
+    MM_CUDA_TRY(cudaGetLastError());
+    mm::count_launch();
     if ((r = check_status(m, s))) return r;
     if (h_loss) {
         float l = 0.0f;
@@ -682,13 +891,13 @@ int mm_mlp_train(mm_mlp m, const void* d_x, const float* d_t, int n, int batch, 
     int cursor = 0;
     for (int k = 0; k < steps; ++k) {
         if (cursor + tiles > total_tiles) cursor = 0;
-        if (h_loss_history) MM_CUDA_TRY(cudaMemsetAsync(m->loss, 0, sizeof(float), s));
         if ((r = run_train(m, d_x, d_t, n, cursor, tiles, 1.0f / (float)(tiles * 128), s))) return r;
         cursor += tiles;
         m->step += 1;
         const float c1 = 1.0f - powf(b1, (float)m->step), c2 = 1.0f - powf(b2, (float)m->step);
-        mm::mlp::adam_kernel<<<(mm::mlp::kParams + 255) / 256, 256, 0, s>>>(m->P, m->WB, m->G, m->M, m->V, lr, b1, b2,
-                                                                           eps, c1, c2);
+        mm::mlp::adam_kernel<<<(mm::mlp::kParams + 256) / 256, 256, 0, s>>>(
+            m->P, m->WB, m->Gp, train_grid(m, tiles), h_loss_history ? m->loss : nullptr, m->M, m->V, lr, b1, b2, eps,
+            c1, c2);
         MM_CUDA_TRY(cudaGetLastError());
         mm::count_launch();
         if (h_loss_history) {
@@ -768,6 +977,22 @@ extern "C" int mm_tc_gemm_check(const void* d_a, const void* d_b, int K, int N, 
     MM_CUDA_TRY(cudaFuncSetAttribute(mlp::tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     mlp::tc_gemm_kernel<<<1, 128, smem, s>>>((const __nv_bfloat16*)d_a, (const __nv_bfloat16*)d_b, K, N, variant,
                                              d_out, d_status);
+    MM_CUDA_TRY(cudaGetLastError());
+    count_launch();
+    return MM_OK;
+}
+
+extern "C" int mm_tc_gemm_mn_check(const void* d_a, const void* d_b, int K, int N, int a_mn, int b_mn, int lbo_k,
+                                   float* d_out, int* d_status, void* stream) {
+    using namespace mm;
+    if (!d_a || !d_b || !d_out || !d_status) return fail(MM_ERR_INVALID_ARGUMENT, "tc gemm: null pointer");
+    if (K < 16 || K > 128 || K % 16 || N < 16 || N > 128 || N % 16)
+        return fail(MM_ERR_INVALID_ARGUMENT, "tc gemm: K and N must be multiples of 16 in [16, 128]");
+    const size_t smem = 3 * 65536;
+    cudaStream_t s = (cudaStream_t)stream;
+    MM_CUDA_TRY(cudaFuncSetAttribute(mlp::tc_gemm_mn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    mlp::tc_gemm_mn_kernel<<<1, 128, smem, s>>>((const __nv_bfloat16*)d_a, (const __nv_bfloat16*)d_b, K, N, a_mn, b_mn,
+                                                lbo_k, d_out, d_status);
     MM_CUDA_TRY(cudaGetLastError());
     count_launch();
     return MM_OK;

@@ -51,7 +51,7 @@ struct mm_context_s {
     // surrogate-cone records (surrogate.cu)
     void* sur_x = nullptr;
     void* sur_meta = nullptr;
-    void* sur_y = nullptr;
+    void* sur_y = nullptr;     // per-ray (l_n, beers mix factor) of the surrogate march
     void* sur_ray = nullptr;
     size_t sur_cap = 0, sur_pixels = 0;
     void* batch = nullptr;  // multi-view launch state (batch.cu)
@@ -109,9 +109,10 @@ int launch_noise(int kind, uint32_t seed, int w, int h, int d, uint8_t* out, cud
 int launch_ref_curl(uint8_t* out_rgba, float* scratch_curl, float* scratch_bounds, cudaStream_t s);
 int launch_hash_stage(int which, const void* in, uint32_t seed, size_t n, void* out, cudaStream_t s);
 
-// Surrogate network (mlp.cu): inference over a sample count held in device memory.
-int mlp_infer_device_count(mm_mlp m, const void* d_x, int cap, const unsigned int* d_count, float* d_y,
-                           cudaStream_t s);
+// Surrogate network (mlp.cu): inference over the deferred cone samples of a surrogate frame (count
+// held in device memory), each prediction added to its ray's transmittance.
+int mlp_infer_accumulate(mm_mlp m, const void* d_x, int cap, const unsigned int* d_count, const float2* meta,
+                         const float2* ray_b, float4* ray_u, cudaStream_t s);
 int* mlp_status_ptr(mm_mlp m);
 
 // Surrogate march and training samples (surrogate.cu).

@@ -10,10 +10,12 @@
 //     T_n = U_n + sum_{k deferred} c_k beers_k exp(l_n - l_k),
 // with c_k = inScatter_k HG (1 - A_{k-1}), l_k = sum_{j=2..k} ln A_{j-1} (l of the ray's last sample
 // is l_n), and U the blend run with y_k = 0 for deferred samples.  The march writes one record per
-// deferred sample (16 BF16 features; ray, c_k, l_k, beers mix factor), the MLP evaluates all
-// records on the tensor cores, an accumulate kernel adds c_k beers_k exp(l_n - l_k) to the ray, and a
-// composite kernel finishes the pixels (compute-clouds.comp:484-499).  A sample that finds the
-// record buffer full takes the plain cone inline.
+// deferred sample: 16 BF16 features (32 B) and (ray, g_k = ln c_k - l_k) (8 B); per ray it keeps
+// (U, accum, rd.y) and (l_n, beers mix factor).  The MLP evaluates all records on the tensor cores
+// and its epilogue adds c_k beers_k exp(l_n - l_k) = beers_k exp(g_k + l_n) to the ray's U (an
+// atomic per record; no prediction goes back to memory), and a composite kernel finishes the pixels
+// (compute-clouds.comp:484-499).  A sample that finds the record buffer full takes the plain cone
+// inline.
 //
 // Features, six-tap set (features6): relative height, low-res density of the sample, cloudTest
 // density at cone taps 0..5, sun direction (3), weather coverage and type at the sample, fractional
@@ -106,9 +108,10 @@ __device__ __forceinline__ float plain_cone(const MarchLaunch& p, const Frame& f
 
 struct Records {
     __nv_bfloat16* X;    // [cap][16] features
-    float4* meta;        // [cap]: ray index (int bits), c_k, l_k, beers mix factor
+    float2* meta;        // [cap]: ray index (int bits), g_k = ln c_k - l_k
     unsigned int* count;
-    float4* ray;         // [height][width]: U, l_n, accum, rd.y
+    float4* ray;         // [height][width]: U, accum, rd.y (rd.y < 0: a killed ray, pixel final)
+    float2* ray_b;       // [height][width]: l_n, beers mix factor -cos(theta)/2 + 1/2
     int cap;
 };
 
@@ -132,11 +135,11 @@ __global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_SUR_MIN_BLOCKS) march_
     const Frame f = make_frame<false>(p);
     Work w;
     const Ray r = ray_setup<false, S>(p, f, px, py);
-    float4* rayrec = rec.ray + (size_t)py * p.width + px;
+    const size_t ray_index = (size_t)py * p.width + px;
     // Background and alpha go to the image now; the composite kernel reads them back.
     store_pixel(p, px, py, make_float4(r.bg.x, r.bg.y, r.bg.z, r.alpha), CUDART_INF_F);
     if (r.killed) {
-        *rayrec = make_float4(1.0f, 0.0f, 0.0f, -1.0f);  // rd.y < 0: the composite leaves the pixel as is
+        rec.ray[ray_index] = make_float4(1.0f, 0.0f, -1.0f, 0.0f);  // rd.y < 0: the composite leaves the pixel
         return;
     }
     const V3 rd = r.rd;
@@ -186,7 +189,7 @@ __global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_SUR_MIN_BLOCKS) march_
                 features(v, f, g, loDensity, da, db, tf.cov, tf.type);
 #endif
                 store_features(rec.X, idx, v);
-                rec.meta[idx] = make_float4(__int_as_float(py * p.width + px), ck, l, mixf_beers);
+                rec.meta[idx] = make_float2(__int_as_float(py * p.width + px), __logf(ck) - l);
                 U = accum * U;  // y_k = 0 in U; the accumulate kernel adds it
             } else {            // buffer full: the plain cone, inline
                 float d6[6];
@@ -212,36 +215,23 @@ __global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_SUR_MIN_BLOCKS) march_
         }
         if (++steps > 100) break;
     }
-    *rayrec = make_float4(U, l, accum, rd.y);
+    rec.ray[ray_index] = make_float4(U, accum, rd.y, 0.0f);
+    rec.ray_b[ray_index] = make_float2(l, mixf_beers);
     if (p.depth) *(reinterpret_cast<float*>(reinterpret_cast<char*>(p.depth) + (size_t)py * p.depth_pitch) + px) = firstT;
     if (C) flush_work(p.counters, w);
-}
-
-// Adds each deferred sample's term c_k beers_k exp(l_n - l_k) to its ray's transmittance.
-__global__ void accumulate_kernel(Records rec, const float* __restrict__ y) {
-    const unsigned n = min(*rec.count, (unsigned)rec.cap);
-    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 m = rec.meta[i];
-        const int ray = __float_as_int(m.x);
-        const float b = y[i];
-        // beers = exp(-dal) = b; beersModulated = max(b, 0.7 exp(-dal / 4)) (:456-460)
-        const float beers = mixf(b, fmaxf(b, 0.7f * sqrtf(sqrtf(b))), m.w);
-        const float ln = rec.ray[ray].y;
-        atomicAdd(&rec.ray[ray].x, m.y * beers * __expf(ln - m.z));
-    }
 }
 
 // Finishes the pixels of a surrogate frame (:484-499).
 __global__ void composite_kernel(MarchLaunch p, Records rec) {
     const int px = blockIdx.x * blockDim.x + threadIdx.x, py = blockIdx.y;
     if (px >= p.width) return;
-    const float4 rr = rec.ray[(size_t)py * p.width + px];
-    if (rr.w < 0.0f) return;  // below the horizon: stored during the march
+    const float4 rr = rec.ray[(size_t)py * p.width + px];  // U, accum, rd.y
+    if (rr.z < 0.0f) return;  // below the horizon: stored during the march
     const Frame f = make_frame<false>(p);
     float4* out = reinterpret_cast<float4*>(reinterpret_cast<char*>(p.rgba) + (size_t)py * p.rgba_pitch) + px;
     const float4 bgA = *out;
-    V3 rd = {0.0f, rr.w, 0.0f};
-    *out = composite<false>(p.u, f, rd, V3{bgA.x, bgA.y, bgA.z}, bgA.w, rr.z, rr.x);
+    V3 rd = {0.0f, rr.z, 0.0f};
+    *out = composite<false>(p.u, f, rd, V3{bgA.x, bgA.y, bgA.z}, bgA.w, rr.y, rr.x);
 }
 
 // ------------------------------------------------------------------------------ training samples
@@ -350,17 +340,18 @@ int launch_surrogate_frame(const MarchLaunch& p, mm_context ctx, mm_mlp net, cud
         ctx->sur_cap = 0;
         ctx->sur_pixels = 0;
         MM_CUDA_TRY(cudaMalloc(&ctx->sur_x, want_cap * kFeatures * sizeof(__nv_bfloat16)));
-        MM_CUDA_TRY(cudaMalloc(&ctx->sur_meta, want_cap * sizeof(float4)));
-        MM_CUDA_TRY(cudaMalloc(&ctx->sur_y, want_cap * sizeof(float)));
+        MM_CUDA_TRY(cudaMalloc(&ctx->sur_meta, want_cap * sizeof(float2)));
+        MM_CUDA_TRY(cudaMalloc(&ctx->sur_y, pixels * sizeof(float2)));  // per-ray (l_n, mix)
         MM_CUDA_TRY(cudaMalloc(&ctx->sur_ray, pixels * sizeof(float4)));
         ctx->sur_cap = want_cap;
         ctx->sur_pixels = pixels;
     }
     Records rec;
     rec.X = (__nv_bfloat16*)ctx->sur_x;
-    rec.meta = (float4*)ctx->sur_meta;
+    rec.meta = (float2*)ctx->sur_meta;
     rec.count = ctx->d_work + 1;
     rec.ray = (float4*)ctx->sur_ray;
+    rec.ray_b = (float2*)ctx->sur_y;
     rec.cap = (int)(ctx->sur_cap < 0x7fffffff ? ctx->sur_cap : 0x7fffffff);
     MM_CUDA_TRY(cudaMemsetAsync(rec.count, 0, sizeof(unsigned int), s));
     dim3 grid((p.width + kBlockTileW - 1) / kBlockTileW, (p.height + kBlockTileH - 1) / kBlockTileH);
@@ -370,13 +361,11 @@ int launch_surrogate_frame(const MarchLaunch& p, mm_context ctx, mm_mlp net, cud
         march_sur_kernel<MM_SAMPLER_HARDWARE, false><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p, rec);
     MM_CUDA_TRY(cudaGetLastError());
     count_launch();
-    int r = mlp_infer_device_count(net, rec.X, rec.cap, rec.count, (float*)ctx->sur_y, s);
+    int r = mlp_infer_accumulate(net, rec.X, rec.cap, rec.count, rec.meta, rec.ray_b, rec.ray, s);
     if (r) return r;
-    accumulate_kernel<<<ctx->num_sms * 8, 256, 0, s>>>(rec, (const float*)ctx->sur_y);
-    MM_CUDA_TRY(cudaGetLastError());
     composite_kernel<<<dim3((p.width + 127) / 128, p.height), 128, 0, s>>>(p, rec);
     MM_CUDA_TRY(cudaGetLastError());
-    count_launch(2);
+    count_launch(1);
     return MM_OK;
 }
 

@@ -46,6 +46,15 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
+// The same with A and/or B read MN-major (bits 15 and 16): the operand's M (or N) index runs
+// along the 16-byte rows of its core matrices and K across the 8 rows.  A tile stored in the
+// K-major layout above as [K][MN] (kmajor_offset(k, mn, MN)) is such an operand, with core-matrix
+// strides 128 bytes along MN and (MN / 8) * 128 bytes along K, so the transpose of a stored
+// activation tile is read in place.
+__host__ __device__ constexpr uint32_t idesc_bf16_mn(int M, int N, bool a_mn, bool b_mn) {
+    return idesc_bf16(M, N) | (a_mn ? (1u << 15) : 0u) | (b_mn ? (1u << 16) : 0u);
+}
+
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
@@ -124,6 +133,17 @@ __device__ __forceinline__ void gemm_mmas(uint32_t d_tmem, uint32_t sa, uint32_t
     const uint32_t idesc = idesc_bf16(128, N);
     for (int kk = 0; kk < K / 16; ++kk)
         mma_bf16(d_tmem, smem_desc(sa + kk * 256, 128, sbo), smem_desc(sb + kk * 256, 128, sbo), idesc, kk > 0 ? 1u : 0u);
+}
+
+// As gemm_mmas, but the first MMA adds to D when `accumulate` is 1 (D += A * B^T): a sum over
+// several launches of the same GEMM shape stays in tensor memory.
+__device__ __forceinline__ void gemm_mmas_acc(uint32_t d_tmem, uint32_t sa, uint32_t sb, int K, int N,
+                                              uint32_t accumulate) {
+    const uint32_t sbo = (uint32_t)(K / 8) * 128;
+    const uint32_t idesc = idesc_bf16(128, N);
+    for (int kk = 0; kk < K / 16; ++kk)
+        mma_bf16(d_tmem, smem_desc(sa + kk * 256, 128, sbo), smem_desc(sb + kk * 256, 128, sbo), idesc,
+                 kk > 0 ? 1u : accumulate);
 }
 
 // gemm_mmas followed by a commit to `bar`.

@@ -164,6 +164,8 @@ SIGNATURES = {
     "mm_kernel_launch_count": (C.c_uint64, []),
     "mm_tc_gemm_check": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                    C.c_void_p]),
+    "mm_tc_gemm_mn_check": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                      C.c_void_p, C.c_void_p, C.c_void_p]),
     "mm_measure_peaks": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double), C.c_void_p]),
     "mm_tc_wait_check": (C.c_int, [C.c_int, C.c_uint, C.c_void_p, C.c_void_p]),
 }

@@ -45,6 +45,31 @@ def test_tc_gemm_layout(cuda, mmlib):
         assert (out.cpu() - ref).abs().max().item() < 1e-4
 
 
+@pytest.mark.parametrize("a_mn,b_mn,K,N", [(1, 0, 128, 80), (0, 1, 128, 80), (1, 1, 128, 32), (0, 1, 64, 64),
+                                            (1, 1, 128, 128)])
+def test_tensor_core_gemm_mn_major_operands(cuda, mmlib, a_mn, b_mn, K, N):
+    # Operands read MN-major from a [K][MN] tile (the training kernel's in-place transposes), with
+    # the K-group stride in the descriptor's leading-byte-offset field.
+    torch = cuda
+    A = (torch.randn(128, K) * 0.5).to(torch.bfloat16)
+    B = (torch.randn(N, K) * 0.5).to(torch.bfloat16)
+    dA = (A.T.contiguous() if a_mn else A).cuda()
+    dB = (B.T.contiguous() if b_mn else B).cuda()
+    ref = A.float() @ B.float().T
+    errs = {}
+    for lbo_k in (1, 0):
+        out = torch.zeros(128, N, device="cuda")
+        st = torch.zeros(1, dtype=torch.int32, device="cuda")
+        assert mmlib.mm_tc_gemm_mn_check(C.c_void_p(dA.data_ptr()), C.c_void_p(dB.data_ptr()), K, N, a_mn, b_mn,
+                                         lbo_k, C.c_void_p(out.data_ptr()), C.c_void_p(st.data_ptr()), None) == 0
+        torch.cuda.synchronize()
+        assert st.item() == 0
+        errs[lbo_k] = (out.cpu() - ref).abs().max().item()
+    print("MN-major a=%d b=%d K=%d N=%d: max error, K stride in LBO %.2e, in SBO %.2e" % (a_mn, b_mn, K, N, errs[1],
+                                                                                          errs[0]))
+    assert errs[1] < 1e-4
+
+
 def test_forward_matches_reference(cuda, mmlib):
     h = _mlp(mmlib, 3)
     try:
@@ -61,12 +86,16 @@ def test_forward_matches_reference(cuda, mmlib):
         mmlib.mm_mlp_destroy(h)
 
 
-def test_gradients_match_reference(cuda, mmlib):
+@pytest.mark.parametrize("n", [700, 128 * 400 + 37])
+def test_gradients_match_reference(cuda, mmlib, n):
+    # n = 700: fewer tiles than CTAs, the last one padded; 51237: every CTA trains on two or more
+    # tiles, so the weight gradients are summed in tensor memory across tiles before the flush.
+    # Per-layer relative error against the float64 reference with the same BF16 rounding points
+    # (measured: 1e-6 .. 3e-4).
     h = _mlp(mmlib, 5)
     try:
         p = _params(mmlib, h)
         rng = np.random.default_rng(2)
-        n = 700  # not a multiple of 128: exercises the padded rows of the last tile
         x = rng.normal(0, 1, (n, 16)).astype(np.float32)
         t = rng.uniform(0.05, 0.95, n).astype(np.float32)
         dx, dt = _bf16_tensor(cuda, x), cuda.from_numpy(t).cuda()
@@ -83,7 +112,7 @@ def test_gradients_match_reference(cuda, mmlib):
             a, b = gg[o:o + k], ref[o:o + k]
             rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
             print("grad %s rel err %.2e" % (name, rel))
-            assert rel < 2e-2, (name, rel)
+            assert rel < 1e-3, (name, rel)
             o += k
     finally:
         mmlib.mm_mlp_destroy(h)

@@ -46,8 +46,8 @@ def trained(cuda, mmlib):
         return float(((y - Te[:ne.value]) ** 2).mean())
 
     before = held_out()
-    for lr, steps in ((3e-3, 1024), (1e-3, 1024)):
-        assert mmlib.mm_mlp_train(h, C.c_void_p(X.data_ptr()), C.c_void_p(T.data_ptr()), n.value, 16384, steps, lr,
+    for lr, steps in ((8e-3, 128), (2.5e-3, 128)):
+        assert mmlib.mm_mlp_train(h, C.c_void_p(X.data_ptr()), C.c_void_p(T.data_ptr()), n.value, 131072, steps, lr,
                                   None, sp) == 0, mmlib.mm_last_error_string()
     after = held_out()
     print("\nsurrogate held-out MSE: untrained %.5f -> trained %.5f (target variance %.5f)" %

@@ -642,6 +642,19 @@ __device__ __forceinline__ float shade(float trans, float accum, float dal, floa
     return mixf(trans, inScatter * hg * beers, 1.0f - accum);
 }
 
+// The blend target inScatter * HG * beersLaw of one accumulated sample (:455-464), the term shade
+// mixes in; the same operations in the same order, so mixf(trans, shade_term(...), 1 - accum)
+// equals shade(...).
+template <bool E>
+__device__ __forceinline__ float shade_term(float dal, float lo, float rh, float cosTheta, float hg) {
+    float beers = M<E>::exp(-dal);
+    float beersMod = fmaxf(beers, 0.7f * M<E>::exp(-0.25f * dal));
+    beers = mixf(beers, beersMod, -cosTheta * 0.5f + 0.5f);
+    float inScatter = 0.09f + M<E>::pow(lo, remapClamped<E>(rh, 0.3f, 0.85f, 0.5f, 2.0f));
+    inScatter *= M<E>::pow(remapClamped<E>(rh, 0.07f, 0.34f, 0.1f, 1.0f), 0.8f);
+    return inScatter * hg * beers;
+}
+
 // End of main() (:484-499): horizon fade, cloud colour, composite.
 template <bool E>
 __device__ __forceinline__ float4 composite(const mm_uniforms& u, const Frame& f, V3 rd, V3 bg, float alpha,
@@ -829,6 +842,9 @@ __device__ __forceinline__ int tile_py(int by, int warp, int lane) {
 #endif
 
 constexpr long long kLatencyRays = 262144;
+#ifndef MM_LATENCY_SCHEDULE
+#define MM_LATENCY_SCHEDULE 1  // launches of at most kLatencyRays rays: 1 = team march, 0 = one thread per ray
+#endif
 
 template <bool E, int S, bool C, int G, bool SC, bool PC = false>
 __device__ __forceinline__ void march_tiled_body(const MarchLaunch& p) {
@@ -869,6 +885,243 @@ __global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_LATENCY_MIN_BLOCKS) ma
     march_tiled_body<E, S, C, 6, (MM_LATENCY_SPEC_CURL != 0), true>(p);
 }
 
+// ------------------------------------------------------------------------------ team march
+//
+// Launches of few rays (a 1920x1080 frame at 1/16 of its pixels) are bound by the chain of
+// dependent texture fetches of their longest rays: a ray just above the horizon takes ~60 large
+// steps, ~200 small steps and ~170 cloudHiRes calls, one after another.  Here a team of kTeam
+// lanes marches one ray.  In a round, member j evaluates the sample the shader's loop would
+// reach j iterations later if nothing changed the step size or the mode: position t + s + ... + s
+// (j additions, as the loop's increments make it), its cloudTest, and in small-step mode its
+// cloudHiRes, sun cone and shading term where the shader would compute them.  The team then runs
+// the loop body (:408-482) sample by sample in order on the shuffled results, every member the
+// same state; a step back (:426-434) or a return to large steps (:468-474) changes the step size,
+// so the rest of the round is dropped and the next round starts where the loop goes on.  Every
+// consumed sample is the computation the sequential loop does, in the same arithmetic, so the
+// output (and the work counts, which count consumed samples only) equals the one-thread march.
+#ifndef MM_TEAM_LANES
+#define MM_TEAM_LANES 4
+#endif
+#ifndef MM_TEAM_MIN_BLOCKS
+#define MM_TEAM_MIN_BLOCKS 4
+#endif
+constexpr int kTeam = MM_TEAM_LANES;
+static_assert(kTeam == 4 || kTeam == 8, "team size");
+// Rays of a warp (32 / kTeam) as a 2x2 (teams of 8) or 4x2 (teams of 4) pixel tile; the four warps
+// of a block side by side in a 2x2 arrangement.
+constexpr int kTeamWarpW = kTeam == 8 ? 2 : 4, kTeamWarpH = 2;
+constexpr int kTeamBlockW = 2 * kTeamWarpW, kTeamBlockH = 2 * kTeamWarpH;
+
+// One ray marched by the calling team (member `member` of the kTeam lanes at `base` of the warp).
+template <bool E, int S, bool C>
+__device__ __forceinline__ void team_ray(const MarchLaunch& p, const Frame& f, const V3* s_cone, int px, int py,
+                                         int member, int base, unsigned tmask) {
+    Work w;
+    const Ray r = ray_setup<E, S>(p, f, px, py);
+    if (r.killed) {
+        if (member == 0) store_pixel(p, px, py, make_float4(r.bg.x, r.bg.y, r.bg.z, r.alpha), CUDART_INF_F);
+        return;
+    }
+    const V3 rd = r.rd;
+    float accum = 0.0f, transmittance = 1.0f;
+    float stepSize = 0.05f * f.thickness;  // :390
+    bool noHits = true;
+    int misses = 0, steps = 0, iterations = 0;
+    float firstT = CUDART_INF_F;
+    float t = r.t0;
+    bool done = false;
+    while (!done) {
+        // ---- this member's sample of the round
+        float tj = t;
+        for (int k = 0; k < member; ++k) tj += stepSize;
+        const bool valid = tj < r.t1 && iterations + member < kMaxIterations;
+        float lo = 0.0f, hi = 0.0f, y = 0.0f;
+        unsigned long long nt = 0, nh = 0;
+        if (valid) {
+            const V3 pos = f.cam + tj * rd;
+            const Geo g = geo_at<E>(f, pos);
+            F4 cu;
+            if (!noHits) cu = curl_fetch<E, S>(p, g);  // issued with the cloudTest fetches
+            lo = cloud_test<E, S>(p, f, g, nt);
+            if (!noHits && lo > 0.0f) {
+                hi = hires_finish<E>(hires_fetch<E, S>(p, curl_displace<E>(g, stepSize, cu)), g.rh, lo, nh);
+                if (hi >= 0.0001f) {
+                    const float dal = cone_taps<E, S, 6, true>(p, f, s_cone, 0, pos, stepSize, 0.0f, nt, nh);
+                    y = shade_term<E>(dal, lo, g.rh, r.cosTheta, r.hg);
+                }
+            }
+        }
+        // ---- the loop body (:408-482) on the round's samples, in order
+#pragma unroll 1
+        for (int i = 0; i < kTeam; ++i) {
+            const bool vi = __shfl_sync(tmask, valid, base + i);
+            if (!vi) {  // the loop condition fails at this iteration: the ray is finished
+                done = true;
+                break;
+            }
+            const float li = __shfl_sync(tmask, lo, base + i);
+            const float hiv = __shfl_sync(tmask, hi, base + i);
+            const float yi = __shfl_sync(tmask, y, base + i);
+            if (C) {
+                w.test += (unsigned)__shfl_sync(tmask, (unsigned)nt, base + i);
+                w.hires += (unsigned)__shfl_sync(tmask, (unsigned)nh, base + i);
+            }
+            ++w.iter;
+            bool restart = false;
+            if (li > 0.0f) {
+                misses = 0;
+                if (noHits) {  // :428-434: back half a step, small steps from here
+                    t -= stepSize;
+                    stepSize *= 0.3f;
+                    noHits = false;
+                    restart = true;
+                } else if (hiv >= 0.0001f) {  // :437-466
+                    transmittance = mixf(transmittance, yi, 1.0f - accum);
+                    ++w.acc;
+                    if (firstT == CUDART_INF_F) firstT = t;
+                    accum += hiv;
+                    if (accum > 0.99f) {  // :476-479
+                        accum = 1.0f;
+                        done = true;
+                        break;
+                    }
+                    if (++steps > 100) {
+                        done = true;
+                        break;
+                    }
+                }
+            } else {
+                if (!noHits) {  // :468-474
+                    misses++;
+                    if (misses >= 10) {
+                        noHits = true;
+                        stepSize = M<E>::div(stepSize, 0.3f);
+                        restart = true;
+                    }
+                }
+                if (++steps > 100) {  // :481
+                    done = true;
+                    break;
+                }
+            }
+            t += stepSize;  // the loop increment (:408), also after a `continue`
+            ++iterations;
+            if (restart) break;
+        }
+    }
+    if (member == 0) {
+        store_pixel(p, px, py, composite<E>(p.u, f, r.rd, r.bg, r.alpha, accum, transmittance), firstT);
+        if (C) flush_work(p.counters, w);
+    }
+}
+
+// Band of ray rows marched by teams, the rest one thread per ray, in one launch: the first
+// team_blocks blocks march kTeamBlockW x kTeamBlockH ray tiles of the band [band0, band1) from its
+// bottom row (the horizon) up, the others 16 x 8 tiles of the rows above the band (nearest first)
+// and then of the rows below it (rays under the horizon, which end at once).
+struct HybridGrid {
+    int team_bx, team_blocks;  // team tiles per band row, team blocks in all
+    int band0, band1;          // ray rows [band0, band1), multiples of 8
+    int single_bx;             // 16-wide tiles per row
+    int rows_above;            // 8-row block rows above the band
+};
+
+template <bool E, int S, bool C>
+__global__ void __launch_bounds__(128, MM_TEAM_MIN_BLOCKS) march_hybrid_kernel(MarchLaunch p, HybridGrid hg) {
+    __shared__ V3 s_cone[6];
+    cone_offsets(p.u, s_cone);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int tx, ty;
+    const bool team_block = (int)blockIdx.x < hg.team_blocks;
+    if (team_block) {
+        const int bx = (int)blockIdx.x % hg.team_bx, byr = (int)blockIdx.x / hg.team_bx;
+        const int team = lane / kTeam;
+        tx = bx * kTeamBlockW + (warp & 1) * kTeamWarpW + team % kTeamWarpW;
+        ty = hg.band1 - kTeamBlockH * (byr + 1) + (warp >> 1) * kTeamWarpH + team / kTeamWarpW;
+    } else {
+        const int idx = (int)blockIdx.x - hg.team_blocks;
+        const int bx = idx % hg.single_bx, k = idx / hg.single_bx;
+        const int row0 = k < hg.rows_above ? hg.band0 - 8 * (k + 1) : hg.band1 + 8 * (k - hg.rows_above);
+        tx = bx * 16 + (warp & 1) * 8 + (lane & 7);
+        ty = row0 + (warp >> 1) * 4 + (lane >> 3);
+    }
+    int px, py;
+    if (p.pixel_mode == MM_PIXELS_PHASE16) {  // :292-298
+        px = tx * 4 + (p.phase % 4);
+        py = ty * 4 + (p.phase / 4);
+    } else {
+        px = tx;
+        py = ty;
+    }
+    if (px >= p.width || py >= p.height) return;  // a team leaves together: its lanes share (px, py)
+    const Frame f = make_frame<E>(p);
+    if (team_block) {
+        const int team = lane / kTeam, base = team * kTeam;
+        team_ray<E, S, C>(p, f, s_cone, px, py, lane % kTeam, base, ((1u << kTeam) - 1u) << base);
+    } else {
+        Work w;
+        march_pixel<E, S, 3, true, true>(p, f, s_cone, px, py, w);
+        if (C) flush_work(p.counters, w);
+    }
+}
+
+// The band for a launch: ray rows whose rays rise at less than MM_TEAM_BAND_DEG degrees (the long
+// ones: at 6 degrees a ray crosses ~190 km of the shell and hits the 100-step limit), widened to
+// multiples of 8 rows and running down to the horizon; a launch of at most MM_TEAM_ALL_RAYS rays
+// marches every row above the horizon by teams.  Empty for a camera with roll (right.y != 0: a
+// row's rays then rise at different angles).  Measured over the 16-frame sweep on GB300, mean
+// ms per launch, against 0.308 (1920x1080 at 1/16) and 0.312 (256x256) one thread per ray:
+//   band 6 deg 0.246 / 0.224, 12 deg 0.264 / 0.193, 25 deg 0.261 / 0.175, every row 0.298 / 0.160.
+// A launch of one wave or less gains from teams everywhere; in a larger one the teams' extra
+// lanes cost more than they save on rays that are not the longest.
+#ifndef MM_TEAM_BAND_DEG
+#define MM_TEAM_BAND_DEG 6
+#endif
+#ifndef MM_TEAM_ALL_RAYS
+#define MM_TEAM_ALL_RAYS 65536
+#endif
+inline HybridGrid hybrid_grid(const MarchLaunch& p, int gw, int gh) {
+    HybridGrid g{};
+    const int ghp = (gh + 7) / 8 * 8;
+    int band0 = ghp, band1 = ghp;
+    const float* v = p.u.camera.view;
+    if (v[4] == 0.0f) {
+        const double cpy = p.u.camera.camera_params[1];
+        const double lx = v[2], ly = v[6], lz = v[10], ux = v[1], uy = v[5], uz = v[9];
+        const double s_band = (long long)gw * gh <= MM_TEAM_ALL_RAYS
+                                  ? 2.0
+                                  : sin((double)MM_TEAM_BAND_DEG * 3.14159265358979323846 / 180.0);
+        const bool phase16 = p.pixel_mode == MM_PIXELS_PHASE16;
+        int first = -1, horizon = gh;
+        for (int ty = 0; ty < gh; ++ty) {
+            const int py = phase16 ? ty * 4 + p.phase / 4 : ty;
+            const double sy = 2.0 * py / p.uv_h - 1.0;
+            // centre-column ray direction (compute-clouds.comp:309-322): -look - sy * tan * up
+            const double dx = -lx - sy * cpy * ux, dy = -ly - sy * cpy * uy, dz = -lz - sy * cpy * uz;
+            const double sin_el = dy / sqrt(dx * dx + dy * dy + dz * dz);
+            if (sin_el <= 0.0) {
+                horizon = ty;
+                break;
+            }
+            if (first < 0 && sin_el < s_band) first = ty;
+        }
+        if (first >= 0 && first < horizon) {
+            band0 = first / 8 * 8;
+            band1 = (horizon + 7) / 8 * 8;
+            if (band1 > ghp) band1 = ghp;
+        }
+    }
+    if (band0 >= band1) band0 = band1 = ghp;  // no band: every row one thread per ray
+    g.band0 = band0;
+    g.band1 = band1;
+    g.team_bx = (gw + kTeamBlockW - 1) / kTeamBlockW;
+    g.team_blocks = g.team_bx * ((band1 - band0) / kTeamBlockH);
+    g.single_bx = (gw + 15) / 16;
+    g.rows_above = band0 / 8;
+    return g;
+}
+
 // Launch order of the block rows.  A ray's cost grows as it nears the horizon (it crosses more of
 // the cloud shell: ~124 km at rd.y = 0 against 20 km straight up) and rays below it end at once,
 // so the rows just above the horizon are the long ones.  Started last, they would form the tail of
@@ -905,7 +1158,14 @@ int launch_tiled(const MarchLaunch& p0, cudaStream_t s) {
     }
     dim3 grid((gw + kBlockTileW - 1) / kBlockTileW, (gh + kBlockTileH - 1) / kBlockTileH);
     p.row_split = horizon_row_split(p, (int)grid.y);
-    if ((long long)gw * gh <= kLatencyRays) {
+    if ((long long)gw * gh <= kLatencyRays && MM_LATENCY_SCHEDULE == 1) {
+        const HybridGrid hg = hybrid_grid(p, gw, gh);
+        const int blocks = hg.team_blocks + hg.single_bx * (hg.rows_above + ((gh + 7) / 8 * 8 - hg.band1) / 8);
+        if (p.counters)
+            march_hybrid_kernel<E, S, true><<<blocks, 128, 0, s>>>(p, hg);
+        else
+            march_hybrid_kernel<E, S, false><<<blocks, 128, 0, s>>>(p, hg);
+    } else if ((long long)gw * gh <= kLatencyRays) {
         if (p.counters)
             march_tiled_latency_kernel<E, S, true><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
         else

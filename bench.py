@@ -56,6 +56,8 @@ def parse_args():
     ap.add_argument("--batch-views", type=int, default=70, help="first N views of the 70-view batch")
     ap.add_argument("--passes-only", action="store_true",
                     help="time only the other passes (one march frame as their input) and print their JSON")
+    ap.add_argument("--small-launches", action="store_true",
+                    help="time only the 1920x1080 1/16-pixel sweep and the 256x256 camera and print their JSON")
     return ap.parse_args()
 
 
@@ -351,6 +353,7 @@ def measure_configs(renderer, textures, flush, stream, with_cpu):
     us = [mm.scene.sweep_uniforms(k, W, H) for k in range(SWEEP)]
     ms1 = sum(_median_ms(lambda: renderer.march(u, textures, rgba, dep), flush, stream, n=3) for u in us) / SWEEP
     out["sweep_1080p"] = {"ms_per_frame": round(ms1, 4), "mrays_per_s": round(W * H / ms1 / 1e3, 1)}
+    out["small_launches"] = measure_small_launches(renderer, textures, flush, stream)
     if with_cpu:
         host = textures.host_all()
         n, dt, th = cpu_march_sample(u0, host, 256, 256, 0, 1)
@@ -366,6 +369,33 @@ def measure_configs(renderer, textures, flush, stream, with_cpu):
                                      "ms_per_frame_estimated": round(1e3 * secs / SWEEP * (W * H * SWEEP / rays), 1),
                                      "sample": "every 2nd row and column of the 16 frames (%.1f s)" % secs}
     return out
+
+
+def measure_small_launches(renderer, textures, flush, stream):
+    """The reference's own per-frame march (compute-clouds.comp dispatched over one pixel in 16 at
+    1920x1080, VulkanApplication.cpp:381-384): the 16 sweep frames, frame k marching phase k,
+    CUDA events, L2 flushed before each launch, median of 5 per frame; and the 256x256 camera."""
+    import torch
+    import marshmallow as mm
+    import marshmallow.lib as L
+    W, H = 1920, 1080
+    rgba = torch.zeros((H, W, 4), device="cuda")
+    dep = torch.zeros((H, W), device="cuda")
+    per = []
+    for k in range(SWEEP):
+        u = mm.scene.sweep_uniforms(k, W, H)
+        u.sun.color[3] = float(k)
+        per.append(_median_ms(lambda: renderer.march(u, textures, rgba, dep, pixel_mode=L.PIXELS_PHASE16), flush,
+                              stream, n=5, warm=2))
+    mean = sum(per) / len(per)
+    u0 = mm.scene.uniforms(256, 256)
+    a = torch.zeros((256, 256, 4), device="cuda")
+    d = torch.zeros((256, 256), device="cuda")
+    ms256 = _median_ms(lambda: renderer.march(u0, textures, a, d), flush, stream, n=5, warm=2)
+    return {"phase16_1080p": {"ms_mean": round(mean, 4), "ms_per_frame": [round(x, 4) for x in per],
+                              "mrays_per_s": round((W // 4) * (H // 4) / mean / 1e3, 1),
+                              "note": "march of the pixels of phase k of sweep frame k (1/16 of 1920x1080)"},
+            "camera_256_ms": round(ms256, 4)}
 
 
 def reference_frame_1080p(renderer, textures, flush, stream, frames=16):
@@ -585,6 +615,15 @@ def run_ours(args):
     for k in range(args.warmup):
         march(k)
     torch.cuda.synchronize()
+
+    if args.small_launches:
+        if rank == 0:
+            print(json.dumps(measure_small_launches(renderer, textures, flush, stream)), flush=True)
+        renderer.close()
+        textures.close()
+        if dist:
+            dist.destroy_process_group()
+        return
 
     if args.passes_only:
         if rank == 0:

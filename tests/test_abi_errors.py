@@ -47,6 +47,7 @@ def _calls(L):
         ("mm_texture_info", (None, C.byref(i), C.byref(i), C.byref(i), C.byref(i), C.byref(i))),
         ("mm_texture_copy_to_host", (None, None, 0)),
         ("mm_texture_set_format", (None, 0, None)),
+        ("mm_texture_sample", (None, None, 4, None, None)),
         ("mm_texture_destroy", (None,)),
         ("mm_march_options_default", (None,)),
         ("mm_context_create", (None,)),
@@ -77,6 +78,7 @@ def _calls(L):
         ("mm_mlp_save", (None, b"/tmp/x")),
         ("mm_mlp_load", (None, b"/tmp/x")),
         ("mm_tc_wait_check", (0, 1024, None, None)),
+        ("mm_tc_gemm_mn_check", (None, None, 128, 64, 1, 1, 1, None, None, None)),
         ("mm_tc_wait_check", (0, 0, C.byref(i), None)),
     ]
 

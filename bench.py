@@ -494,7 +494,8 @@ def train_surrogate(lib, stream):
 
 def measure_variants(lib, renderer, textures, w, h, flush, stream, with_oracle):
     """BASELINE's metric itself: the 3840x2160 sweep for each variant of the march -- plain with
-    UNORM8 (the reference's texel format), FP16 or BF16 density textures, and the learned
+    UNORM8 (the reference's texel format), FP16 (also with the large-step coverage test in half2)
+    or BF16 density textures, and the learned
     sun-cone surrogate with UNORM8 or FP16 density -- each with its ms/frame (CUDA events, L2 flushed
     before every frame, mean over the 16 sweep frames) and its error against the FP64 oracle (exact
     filter weights) on a fixed grid (every 8th row and column, sweep frames 0, 5, 10, 15)."""
@@ -505,7 +506,7 @@ def measure_variants(lib, renderer, textures, w, h, flush, stream, with_oracle):
     net, training = train_surrogate(lib, stream)
     variants = [("plain_unorm8", L.FORMAT_UNORM8, None), ("surrogate_unorm8", L.FORMAT_UNORM8, net.value),
                 ("plain_fp16", L.FORMAT_FP16, None), ("surrogate_fp16", L.FORMAT_FP16, net.value),
-                ("plain_bf16", L.FORMAT_BF16, None)]
+                ("plain_fp16_half2", L.FORMAT_FP16, None), ("plain_bf16", L.FORMAT_BF16, None)]
     err_frames = (0, 5, 10, 15)
     refs = {}
     if with_oracle:
@@ -523,6 +524,8 @@ def measure_variants(lib, renderer, textures, w, h, flush, stream, with_oracle):
         for name, fmt, sur in variants:
             textures.set_density_format(fmt)
             opts = dict(density_format=fmt, surrogate=sur)
+            if name.endswith("half2"):
+                opts["math"] = L.MATH_FAST_HALF2  # large-step coverage test in half2
             for k in range(SWEEP):
                 renderer.march(frame_uniforms(k, w, h), textures, rgba, dep, **opts)
             ts = []
@@ -558,6 +561,7 @@ def measure_variants(lib, renderer, textures, w, h, flush, stream, with_oracle):
     plain = out["plain_unorm8"]["ms_per_frame"]
     summary = {"surrogate_fp16_vs_plain_speedup": round(plain / out["surrogate_fp16"]["ms_per_frame"], 4),
                "fp16_vs_plain_speedup": round(plain / out["plain_fp16"]["ms_per_frame"], 4),
+               "fp16_half2_vs_plain_speedup": round(plain / out["plain_fp16_half2"]["ms_per_frame"], 4),
                "surrogate_fp16_rmse_255_max": out["surrogate_fp16"].get("rmse_255_max"),
                "error_yardstick": "FP64 oracle, exact filter weights, every 8th row and column of sweep frames "
                                   "0, 5, 10, 15" if refs else None}

@@ -264,6 +264,11 @@ typedef enum mm_sampler_mode {
 
 typedef enum mm_math_mode {
     MM_MATH_FAST = 0,  /* FMA contraction and hardware transcendental approximations */
+    MM_MATH_FAST_HALF2 = 2, /* MM_MATH_FAST with the large-step coverage test (the density > 0
+                               decision of a large step, compute-clouds.comp:421-426) made in half2
+                               on pairs of consecutive samples from FP16 texels; transmittance,
+                               phase and in-scatter stay FP32.  Full frames with FP16/BF16 density,
+                               hardware sampler, tiled schedule only. */
     MM_MATH_EXACT = 1  /* IEEE +,-,*,/,sqrt without contraction and the library's own
                           elementary functions: reproduces the FP32 CPU oracle bit for bit
                           when combined with MM_SAMPLER_SOFTWARE */

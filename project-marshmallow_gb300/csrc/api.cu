@@ -470,7 +470,12 @@ int mm::validate_march(mm_context ctx, const mm_uniforms* u, const mm_scene_text
         return fail(MM_ERR_INVALID_ARGUMENT, "march: bad pixel_mode %d", o.pixel_mode);
     if (o.sampler != MM_SAMPLER_HARDWARE && o.sampler != MM_SAMPLER_SOFTWARE)
         return fail(MM_ERR_INVALID_ARGUMENT, "march: bad sampler %d", o.sampler);
-    if (o.math != MM_MATH_FAST && o.math != MM_MATH_EXACT) return fail(MM_ERR_INVALID_ARGUMENT, "march: bad math %d", o.math);
+    if (o.math != MM_MATH_FAST && o.math != MM_MATH_EXACT && o.math != MM_MATH_FAST_HALF2)
+        return fail(MM_ERR_INVALID_ARGUMENT, "march: bad math %d", o.math);
+    if (o.math == MM_MATH_FAST_HALF2 &&
+        (o.density_format == MM_FORMAT_UNORM8 || o.sampler != MM_SAMPLER_HARDWARE || o.schedule != MM_SCHEDULE_TILED))
+        return fail(MM_ERR_INVALID_ARGUMENT,
+                    "march: the half2 coverage test needs FP16/BF16 density, the hardware sampler and the tiled schedule");
     if (o.schedule != MM_SCHEDULE_PERSISTENT && o.schedule != MM_SCHEDULE_TILED)
         return fail(MM_ERR_INVALID_ARGUMENT, "march: bad schedule %d", o.schedule);
     if (o.cone != MM_CONE_PLAIN && o.cone != MM_CONE_SURROGATE) return fail(MM_ERR_INVALID_ARGUMENT, "march: bad cone %d", o.cone);
@@ -564,7 +569,8 @@ int mm_clouds_march(mm_context ctx, const mm_uniforms* u, const mm_scene_texture
     if (o.cone == MM_CONE_SURROGATE && u->sun.direction[1] >= 0.0f)
         return mm::launch_surrogate_frame(p, ctx, o.surrogate, s);
     if (o.math == MM_MATH_EXACT) return mm::launch_march_exact(p, o.sampler, o.schedule, ctx->d_work, ctx->num_sms, s);
-    return mm::launch_march_fast(p, o.sampler, o.density_format, o.schedule, ctx->d_work, ctx->num_sms, s);
+    return mm::launch_march_fast(p, o.sampler, o.density_format, o.schedule, o.math == MM_MATH_FAST_HALF2, ctx->d_work,
+                                 ctx->num_sms, s);
 }
 
 }  // extern "C"

@@ -188,7 +188,7 @@ int capture_views(mm_context ctx, BatchState* b, const mm_view* views, int n, co
         mo.coverage_offset = v.coverage_offset;
         mm::MarchLaunch p;
         mm::fill_march_launch(v.u, tex, v.out, mo, &p);
-        r = mm::launch_march_fast(p, MM_SAMPLER_HARDWARE, MM_FORMAT_UNORM8, MM_SCHEDULE_TILED, ctx->d_work, ctx->num_sms,
+        r = mm::launch_march_fast(p, MM_SAMPLER_HARDWARE, MM_FORMAT_UNORM8, MM_SCHEDULE_TILED, 0, ctx->d_work, ctx->num_sms,
                                   b->branch[i % K]);
     }
     for (int k = 1; k < K; ++k) {

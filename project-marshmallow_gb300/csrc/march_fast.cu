@@ -4,12 +4,13 @@
 
 namespace mm {
 
-int launch_march_fast(const MarchLaunch& p, int sampler, int format, int schedule, unsigned int* work, int num_sms,
-                      cudaStream_t s) {
+int launch_march_fast(const MarchLaunch& p, int sampler, int format, int schedule, int half2, unsigned int* work,
+                      int num_sms, cudaStream_t s) {
     (void)format;
     if (schedule == MM_SCHEDULE_TILED) {
         if (sampler == MM_SAMPLER_SOFTWARE) return march::launch_tiled<false, MM_SAMPLER_SOFTWARE>(p, s);
-        return march::launch_tiled<false, MM_SAMPLER_HARDWARE>(p, s);
+        // MM_MATH_FAST_HALF2 (FP16/BF16 density): full frames make their large-step decisions in half2
+        return march::launch_tiled<false, MM_SAMPLER_HARDWARE>(p, s, half2 != 0);
     }
     if (sampler == MM_SAMPLER_SOFTWARE)
         return march::launch_persistent<false, MM_SAMPLER_SOFTWARE>(p, work, num_sms, s);

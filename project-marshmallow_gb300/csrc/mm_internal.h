@@ -101,8 +101,8 @@ struct MarchLaunch {
 // Kernel launchers (one translation unit per arithmetic mode).
 int launch_march_exact(const MarchLaunch& p, int sampler, int schedule, unsigned int* work, int num_sms,
                        cudaStream_t s);
-int launch_march_fast(const MarchLaunch& p, int sampler, int format, int schedule, unsigned int* work, int num_sms,
-                      cudaStream_t s);
+int launch_march_fast(const MarchLaunch& p, int sampler, int format, int schedule, int half2, unsigned int* work,
+                      int num_sms, cudaStream_t s);
 
 // Noise generators (noise.cu).
 int launch_noise(int kind, uint32_t seed, int w, int h, int d, uint8_t* out, cudaStream_t s);

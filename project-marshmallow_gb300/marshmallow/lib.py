@@ -21,7 +21,7 @@ NOISE_LOWRES, NOISE_HIRES, NOISE_CURL2D, NOISE_WEATHER, NOISE_REF_CURL = range(5
 FORMAT_UNORM8, FORMAT_FP16, FORMAT_BF16 = range(3)
 PIXELS_FULL, PIXELS_PHASE16 = range(2)
 SAMPLER_HARDWARE, SAMPLER_SOFTWARE = range(2)
-MATH_FAST, MATH_EXACT = range(2)
+MATH_FAST, MATH_EXACT, MATH_FAST_HALF2 = range(3)
 BATCH_PERSISTENT, BATCH_BLOCKS, BATCH_GRAPH = range(3)
 SCHEDULE_TILED, SCHEDULE_PERSISTENT = range(2)
 CONE_PLAIN, CONE_SURROGATE = range(2)

@@ -151,6 +151,24 @@ def test_size_limits(cuda, mmlib, env):
     cuda.cuda.synchronize()
 
 
+def test_half2_coverage_test_needs_fp16_density(cuda, mmlib, env):
+    # MM_MATH_FAST_HALF2 reads the density texels as packed FP16: with UNORM8 density, the software
+    # sampler or the persistent schedule it is rejected before any launch.
+    import marshmallow as mm
+    import marshmallow.lib as L
+    tex, r = env
+    u = mm.scene.uniforms(64, 64)
+    buf = cuda.zeros((64, 64, 4), device="cuda")
+    img = L.Image(buf.data_ptr(), 64 * 16, None, 0, 64, 64)
+    st = tex.scene()
+    for kw in (dict(), dict(density_format=L.FORMAT_FP16, sampler=L.SAMPLER_SOFTWARE),
+               dict(density_format=L.FORMAT_FP16, schedule=L.SCHEDULE_PERSISTENT)):
+        o = r.options(math=L.MATH_FAST_HALF2, **kw)
+        assert mmlib.mm_clouds_march(r.ctx, C.byref(u), C.byref(st), C.byref(img), C.byref(o), None) == \
+            L.MM_ERR_INVALID_ARGUMENT, kw
+    cuda.cuda.synchronize()
+
+
 def test_kernel_variants_exact(cuda, orc, oracle_textures, env):
     # The march picks one of three kernels per launch (full frames, launches of <= 262144 rays,
     # larger 1/16-pixel launches); all three are the same arithmetic and equal the oracle bit for bit.

@@ -25,12 +25,14 @@ def setup(cuda, mmlib):
     t.close()
 
 
-@pytest.mark.parametrize("fmt", ["unorm8", "fp16", "bf16"])
+@pytest.mark.parametrize("fmt", ["unorm8", "fp16", "bf16", "fp16_half2"])
 def test_precision_sweep_4k(cuda, orc, setup, fmt):
+    # fp16_half2: FP16 density with the large-step coverage test in half2 (MM_MATH_FAST_HALF2)
     import marshmallow as mm
     import marshmallow.lib as L
     tex, r, host = setup
-    f = {"unorm8": L.FORMAT_UNORM8, "fp16": L.FORMAT_FP16, "bf16": L.FORMAT_BF16}[fmt]
+    f = {"unorm8": L.FORMAT_UNORM8, "fp16": L.FORMAT_FP16, "bf16": L.FORMAT_BF16, "fp16_half2": L.FORMAT_FP16}[fmt]
+    math = L.MATH_FAST_HALF2 if fmt == "fp16_half2" else L.MATH_FAST
     tex.set_density_format(f)
     rows = []
     try:
@@ -38,7 +40,7 @@ def test_precision_sweep_4k(cuda, orc, setup, fmt):
             for off in (-0.2, 0.0, 0.2):
                 p = mm.scene.sweep_params(0)
                 u = mm.scene.uniforms(W, H, yaw=p["yaw"], pitch=p["pitch"], time=p["time"], sun_elevation=el)
-                rgba, dep = render(cuda, r, u, tex, W, H, density_format=f, coverage_offset=off)
+                rgba, dep = render(cuda, r, u, tex, W, H, density_format=f, coverage_offset=off, math=math)
                 ref, rdep, _ = orc.march(u, host, W, H, precision=64, coverage_offset=off, rows=(3, H, STEP),
                                          col_begin=3, col_step=STEP)
                 e = mm.metrics.frame_errors(rgba[3::STEP, 3::STEP], ref, dep[3::STEP, 3::STEP], rdep)
@@ -51,7 +53,7 @@ def test_precision_sweep_4k(cuda, orc, setup, fmt):
               e["max_255"], e["frac_over_4"], e["depth_rel_median"], e["depth_frac_over_1e3"]))
     for el, off, e in rows:
         assert e["nan"] == 0
-        if fmt == "fp16":
+        if fmt in ("fp16", "fp16_half2"):
             assert e["rmse_255"] <= 2.0, (el, off, e)
             assert e["frac_over_4"] <= 0.005, (el, off, e)
         elif fmt == "bf16":

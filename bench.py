@@ -492,7 +492,7 @@ def train_surrogate(lib, stream):
                  "note": "one-off cost per texture set, not part of a frame"}
 
 
-def measure_variants(lib, renderer, textures, w, h, flush, stream, with_oracle):
+def measure_variants(lib, renderer, textures, w, h, flush, stream, with_oracle, net, training):
     """BASELINE's metric itself: the 3840x2160 sweep for each variant of the march -- plain with
     UNORM8 (the reference's texel format), FP16 (also with the large-step coverage test in half2)
     or BF16 density textures, and the learned
@@ -503,7 +503,6 @@ def measure_variants(lib, renderer, textures, w, h, flush, stream, with_oracle):
     import torch
     import marshmallow as mm
     import marshmallow.lib as L
-    net, training = train_surrogate(lib, stream)
     variants = [("plain_unorm8", L.FORMAT_UNORM8, None), ("surrogate_unorm8", L.FORMAT_UNORM8, net.value),
                 ("plain_fp16", L.FORMAT_FP16, None), ("surrogate_fp16", L.FORMAT_FP16, net.value),
                 ("plain_fp16_half2", L.FORMAT_FP16, None), ("plain_bf16", L.FORMAT_BF16, None)]
@@ -557,7 +556,6 @@ def measure_variants(lib, renderer, textures, w, h, flush, stream, with_oracle):
             out[name] = d
     finally:
         textures.set_density_format(L.FORMAT_UNORM8)
-        lib.mm_mlp_destroy(net)
     plain = out["plain_unorm8"]["ms_per_frame"]
     summary = {"surrogate_fp16_vs_plain_speedup": round(plain / out["surrogate_fp16"]["ms_per_frame"], 4),
                "fp16_vs_plain_speedup": round(plain / out["plain_fp16"]["ms_per_frame"], 4),
@@ -753,8 +751,15 @@ def run_ours(args):
         configs = measure_configs(renderer, textures, flush, stream, not args.no_cpu_baseline)
 
     variants = None
+    batch = None
     if rank == 0 and world == 1 and not args.no_variants:
-        variants = measure_variants(lib, renderer, textures, w, h, flush, stream, not args.no_cpu_baseline)
+        net, training = train_surrogate(lib, stream)
+        try:
+            variants = measure_variants(lib, renderer, textures, w, h, flush, stream, not args.no_cpu_baseline, net,
+                                        training)
+            batch = measure_batch(renderer, textures, net.value, flush, stream, steps=3, warmup=2)
+        finally:
+            lib.mm_mlp_destroy(net)
 
     passes = None
     if rank == 0 and not args.no_passes:
@@ -783,7 +788,7 @@ def run_ours(args):
             "work_per_frame": {"cloud_test": n_test / args.steps, "cloud_hires": n_hires / args.steps,
                                "iterations": n_iter / args.steps, "accumulated": n_acc / args.steps},
             "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks, "cpu_baseline": cpu,
-            "configs": configs, "variants": variants, "passes": passes,
+            "configs": configs, "variants": variants, "batch": batch, "passes": passes,
         }
         print(json.dumps(line), flush=True)
     renderer.close()
@@ -792,11 +797,64 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def run_batch(args):
+def measure_batch(renderer, tex, net, flush, stream, steps, warmup, n_views=70):
     """Many views in one launch: the seeded 70-view batch (6 cube-map faces at 512^2, 32 cameras at
-    640x360-1920x1080, 32 cameras at 3840x2160 with random sun and yaw), one mm_clouds_march_batch
-    per step with the schedule and tile shape the autotuner picks; beside it the same views as one
-    launch each."""
+    640x360-1920x1080, 32 cameras at 3840x2160 with random sun and yaw).  Plain cone with UNORM8
+    density: one mm_clouds_march_batch per step with the schedule and tile shape the autotuner
+    picks, beside the same views as one launch each.  With a trained surrogate (`net`): the batch of
+    the mixed-precision learned configuration -- surrogate cone, FP16 density, graph schedule."""
+    import torch
+    import marshmallow as mm
+    import marshmallow.lib as L
+    lib = mm.lib.load()
+    views = mm.scene.batch_views(seed=0)[:max(1, n_views)]
+    outs = [(torch.empty((h, w, 4), device="cuda"), torch.empty((h, w), device="cuda")) for w, h, _ in views]
+    rays = sum(w * h for w, h, _ in views)
+    arr = renderer.march_batch(views, tex, outs)
+    best, table = renderer.autotune_batch(arr, len(views), tex)
+    opts = dict(warp_tile_w=best.warp_tile_w, tiles_per_grab=best.tiles_per_grab, schedule=best.schedule)
+
+    def timed(fn, k):
+        ts = []
+        for i in range(warmup + k):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            if i >= warmup:
+                ts.append(a.elapsed_time(b))
+        return sum(ts) / len(ts)
+
+    l0 = lib.mm_kernel_launch_count()
+    ms = timed(lambda: renderer.march_batch(views, tex, outs, **opts), steps)
+    launches = lib.mm_kernel_launch_count() - l0
+    ms_seq = timed(lambda: [renderer.march(u, tex, o[0], o[1]) for (w, h, u), o in zip(views, outs)], max(1, steps // 4))
+    out = {"views": len(views), "mrays_per_step": round(rays / 1e6, 2),
+           "plain_unorm8": {"ms": round(ms, 3), "mrays_per_s": round(rays / ms / 1e3, 1),
+                            "schedule": {0: "persistent", 1: "blocks", 2: "graph"}[best.schedule],
+                            "warp_tile_w": best.warp_tile_w, "tiles_per_grab": best.tiles_per_grab,
+                            "gpu_launches_per_step": int(launches) // max(1, warmup + steps)},
+           "one_launch_per_view_ms": round(ms_seq, 3), "autotune_ms": [round(v, 2) for v in table],
+           "l2": "flushed between steps"}
+    if net is not None:
+        tex.set_density_format(L.FORMAT_FP16)
+        try:
+            sur = dict(density_format=L.FORMAT_FP16, surrogate=net, schedule=L.BATCH_GRAPH)
+            ms_s = timed(lambda: renderer.march_batch(views, tex, outs, **sur), steps)
+            ms_f = timed(lambda: renderer.march_batch(views, tex, outs, density_format=L.FORMAT_FP16,
+                                                      schedule=L.BATCH_GRAPH), steps)
+        finally:
+            tex.set_density_format(L.FORMAT_UNORM8)
+        out["surrogate_fp16"] = {"ms": round(ms_s, 3), "mrays_per_s": round(rays / ms_s / 1e3, 1),
+                                 "schedule": "graph (surrogate views one after another)"}
+        out["plain_fp16"] = {"ms": round(ms_f, 3), "mrays_per_s": round(rays / ms_f / 1e3, 1), "schedule": "graph"}
+    return out
+
+
+def run_batch(args):
+    """The batch alone as its own JSON line (`python bench.py --batch`)."""
     import torch
     import marshmallow as mm
     rank, world, local = rank_info()
@@ -805,48 +863,20 @@ def run_batch(args):
         return
     tex = mm.render.Textures(seed=0)
     r = mm.render.Renderer()
-    views = mm.scene.batch_views(seed=0)[:max(1, args.batch_views)]
-    outs = [(torch.empty((h, w, 4), device="cuda"), torch.empty((h, w), device="cuda")) for w, h, _ in views]
-    rays = sum(w * h for w, h, _ in views)
-    arr = r.march_batch(views, tex, outs)
-    best, table = r.autotune_batch(arr, len(views), tex)
-    opts = dict(warp_tile_w=best.warp_tile_w, tiles_per_grab=best.tiles_per_grab, schedule=best.schedule)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    stream = torch.cuda.current_stream()
-
-    def timed(fn, k):
-        ts = []
-        for i in range(args.warmup + k):
-            flush.zero_()
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            fn()
-            b.record(stream)
-            torch.cuda.synchronize()
-            if i >= args.warmup:
-                ts.append(a.elapsed_time(b))
-        return ts
-
-    lib = mm.lib.load()
-    l0 = lib.mm_kernel_launch_count()
-    ts = timed(lambda: r.march_batch(views, tex, outs, **opts), args.steps)
-    launches = lib.mm_kernel_launch_count() - l0
-    seq = timed(lambda: [r.march(u, tex, o[0], o[1]) for (w, h, u), o in zip(views, outs)], max(1, args.steps // 4))
-    ms = sum(ts) / len(ts)
-    ms_seq = sum(seq) / len(seq)
+    b = measure_batch(r, tex, None, flush, torch.cuda.current_stream(), args.steps, args.warmup, args.batch_views)
+    p = b["plain_unorm8"]
     line = {
-        "metric": "Mrays/s, %d views of uneven resolution in one batched launch" % len(views),
-        "value": round(rays / ms / 1e3, 2),
-        "unit": "Mrays/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "metric": "Mrays/s, %d views of uneven resolution in one batched launch" % b["views"],
+        "value": p["mrays_per_s"], "unit": "Mrays/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": p["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
         "config": {"workload": "seeded uneven-view batch (cube faces 512^2, 640x360-1920x1080 cameras, 3840x2160 "
-                               "cameras with random sun 5-85 deg and yaw 0-360 deg)", "views": len(views),
-                   "mrays_per_step": round(rays / 1e6, 2),
-                   "schedule": {0: "persistent", 1: "blocks", 2: "graph"}[best.schedule],
-                   "warp_tile_w": best.warp_tile_w, "tiles_per_grab": best.tiles_per_grab,
-                   "l2": "flushed between steps"},
-        "one_launch_per_view_ms": round(ms_seq, 3), "autotune_ms": [round(v, 2) for v in table],
-        "gpu_launches": int(launches),
+                               "cameras with random sun 5-85 deg and yaw 0-360 deg)", "views": b["views"],
+                   "mrays_per_step": b["mrays_per_step"], "schedule": p["schedule"], "warp_tile_w": p["warp_tile_w"],
+                   "tiles_per_grab": p["tiles_per_grab"], "l2": "flushed between steps"},
+        "one_launch_per_view_ms": b["one_launch_per_view_ms"], "autotune_ms": b["autotune_ms"],
+        "gpu_launches": p["gpu_launches_per_step"] * args.steps,
     }
     print(json.dumps(line), flush=True)
     r.close()

@@ -431,11 +431,15 @@ typedef struct mm_batch_options {
     int tiles_per_grab; /* persistent schedule: warp tiles taken from the queue at a time, 1..64 (default 4) */
     int use_graph;      /* 1 (default): replay a captured CUDA graph (upload, reset, kernel) */
     int schedule;       /* mm_batch_schedule (default MM_BATCH_GRAPH, the fastest on the 70-view batch) */
+    int density_format; /* mm_texel_format of the density textures' hardware copies (default UNORM8) */
+    mm_mlp surrogate;   /* non-NULL: the learned sun cone for every view with the sun above the horizon
+                           (MM_BATCH_GRAPH only; such views run one after another, sharing the
+                           context's deferred-sample records) */
 } mm_batch_options;
 
 int mm_batch_options_default(mm_batch_options* o);
 
-/* Renders n views (full frames, hardware sampler, fast math, plain cone) with the shared textures:
+/* Renders n views (full frames, hardware sampler, fast math, plain or surrogate cone) with the shared textures:
  * blocks of all views in one grid (MM_BATCH_BLOCKS; one launch per 72 views), a persistent kernel
  * whose warps take tiles of all views from one queue (MM_BATCH_PERSISTENT), or one CUDA graph of the
  * views' own launches on concurrent branches (MM_BATCH_GRAPH, re-captured and updated in place on

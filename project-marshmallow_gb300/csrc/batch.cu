@@ -151,7 +151,7 @@ struct BatchState {
 // Views in order of decreasing ray count, dealt round-robin to the graph's branches (the longest
 // launches start first on every branch; the small ones fill the others' tails).
 int capture_views(mm_context ctx, BatchState* b, const mm_view* views, int n, const mm_scene_textures* tex,
-                  cudaGraph_t* out) {
+                  const mm_batch_options& o, cudaGraph_t* out) {
     constexpr int K = BatchState::kBranches;
     if (!b->fork) {
         MM_CUDA_TRY(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
@@ -186,10 +186,16 @@ int capture_views(mm_context ctx, BatchState* b, const mm_view* views, int n, co
         mm_march_options mo;
         mm_march_options_default(&mo);
         mo.coverage_offset = v.coverage_offset;
+        mo.density_format = o.density_format;
         mm::MarchLaunch p;
         mm::fill_march_launch(v.u, tex, v.out, mo, &p);
-        r = mm::launch_march_fast(p, MM_SAMPLER_HARDWARE, MM_FORMAT_UNORM8, MM_SCHEDULE_TILED, 0, ctx->d_work, ctx->num_sms,
-                                  b->branch[i % K]);
+        // Surrogate views share the context's records: they run one after another on branch 0.  A
+        // view with the sun below the horizon takes the plain cone, as a single march does.
+        if (o.surrogate && v.u.sun.direction[1] >= 0.0f)
+            r = mm::launch_surrogate_frame(p, ctx, o.surrogate, b->branch[0]);
+        else
+            r = mm::launch_march_fast(p, MM_SAMPLER_HARDWARE, o.density_format, MM_SCHEDULE_TILED, 0, ctx->d_work,
+                                      ctx->num_sms, b->branch[o.surrogate ? 0 : i % K]);
     }
     for (int k = 1; k < K; ++k) {
         cudaEventRecord(b->join[k], b->branch[k]);
@@ -315,11 +321,18 @@ extern "C" int mm_clouds_march_batch(mm_context ctx, const mm_view* views, int n
         return fail(MM_ERR_INVALID_ARGUMENT, "batch: tiles_per_grab must be in [1, 64]");
     if (o.schedule != MM_BATCH_BLOCKS && o.schedule != MM_BATCH_PERSISTENT && o.schedule != MM_BATCH_GRAPH)
         return fail(MM_ERR_INVALID_ARGUMENT, "batch: bad schedule %d", o.schedule);
+    if (o.surrogate && o.schedule != MM_BATCH_GRAPH)
+        return fail(MM_ERR_INVALID_ARGUMENT, "batch: the surrogate cone needs the graph schedule");
     // Validate textures and images as a single-view march would, through its own checks.
     for (int i = 0; i < n; ++i) {
         mm_march_options mo;
         mm_march_options_default(&mo);
         mo.coverage_offset = views[i].coverage_offset;
+        mo.density_format = o.density_format;
+        if (o.surrogate) {
+            mo.cone = MM_CONE_SURROGATE;
+            mo.surrogate = o.surrogate;
+        }
         int r = mm::validate_march(ctx, &views[i].u, tex, &views[i].out, &mo);
         if (r) {
             char msg[400];
@@ -339,7 +352,16 @@ extern "C" int mm_clouds_march_batch(mm_context ctx, const mm_view* views, int n
         // Each view's own launch (its kernel variant, uniforms by value) captured on the branches,
         // then applied to the executable graph (cudaGraphExecUpdate) or instantiated anew.
         cudaGraph_t g = nullptr;
-        int r = capture_views(ctx, b, views, n, tex, &g);
+        if (o.surrogate) {  // the deferred-sample records of the largest view, allocated before the capture
+            size_t most = 0;
+            for (int i = 0; i < n; ++i) {
+                const size_t px = (size_t)views[i].out.width * views[i].out.height;
+                if (px > most) most = px;
+            }
+            int rr = mm::surrogate_reserve(ctx, most);
+            if (rr) return rr;
+        }
+        int r = capture_views(ctx, b, views, n, tex, o, &g);
         if (r) return r;
         bool updated = false;
         if (b->exec && b->g_sched == MM_BATCH_GRAPH && b->g_n == n) {

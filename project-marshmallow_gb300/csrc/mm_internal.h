@@ -117,6 +117,9 @@ int* mlp_status_ptr(mm_mlp m);
 
 // Surrogate march and training samples (surrogate.cu).
 int launch_surrogate_frame(const MarchLaunch& p, mm_context ctx, mm_mlp net, cudaStream_t s);
+// Allocates the context's deferred-sample records for frames of up to `pixels` pixels (no-op if
+// they are large enough): a surrogate frame launched during a stream capture must find them there.
+int surrogate_reserve(mm_context ctx, size_t pixels);
 int launch_surrogate_samples(const MarchLaunch& p, uint32_t seed, unsigned long long first, unsigned long long n,
                              float half_extent, void* d_x, float* d_t, unsigned int* d_count, int cap,
                              cudaStream_t s);

@@ -323,9 +323,8 @@ __global__ void __launch_bounds__(128) sample_kernel(SampleParams sp, unsigned l
 
 }  // namespace sur
 
-int launch_surrogate_frame(const MarchLaunch& p, mm_context ctx, mm_mlp net, cudaStream_t s) {
+int surrogate_reserve(mm_context ctx, size_t pixels) {
     using namespace sur;
-    const size_t pixels = (size_t)p.width * p.height;
     // Record capacity: 4 per pixel (a 4K frame of the benchmark sweep defers ~3 per marched ray).
     const size_t want_cap = pixels * 4;
     if (ctx->sur_cap < want_cap || ctx->sur_pixels < pixels) {
@@ -346,6 +345,14 @@ int launch_surrogate_frame(const MarchLaunch& p, mm_context ctx, mm_mlp net, cud
         ctx->sur_cap = want_cap;
         ctx->sur_pixels = pixels;
     }
+    return MM_OK;
+}
+
+int launch_surrogate_frame(const MarchLaunch& p, mm_context ctx, mm_mlp net, cudaStream_t s) {
+    using namespace sur;
+    const size_t pixels = (size_t)p.width * p.height;
+    int rr = surrogate_reserve(ctx, pixels);
+    if (rr) return rr;
     Records rec;
     rec.X = (__nv_bfloat16*)ctx->sur_x;
     rec.meta = (float2*)ctx->sur_meta;

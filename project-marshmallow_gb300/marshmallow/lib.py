@@ -93,7 +93,8 @@ class View(C.Structure):
 
 
 class BatchOptions(C.Structure):
-    _fields_ = [("warp_tile_w", C.c_int), ("tiles_per_grab", C.c_int), ("use_graph", C.c_int), ("schedule", C.c_int)]
+    _fields_ = [("warp_tile_w", C.c_int), ("tiles_per_grab", C.c_int), ("use_graph", C.c_int), ("schedule", C.c_int),
+                ("density_format", C.c_int), ("surrogate", C.c_void_p)]
 
 
 # Every function include/mm.h declares, with its ctypes signature.

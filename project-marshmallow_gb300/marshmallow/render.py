@@ -211,15 +211,16 @@ class Renderer:
                 "mm_post_chain")
 
     def march_batch(self, views, textures, outputs, stream=None, warp_tile_w=8, tiles_per_grab=4, use_graph=1,
-                    schedule=L.BATCH_GRAPH):
-        """views: (width, height, uniforms) triples; outputs: matching (rgba, depth) CUDA tensors."""
+                    schedule=L.BATCH_GRAPH, density_format=L.FORMAT_UNORM8, surrogate=None):
+        """views: (width, height, uniforms) triples; outputs: matching (rgba, depth) CUDA tensors;
+        surrogate: a trained mm_mlp handle for the learned sun cone (graph schedule)."""
         arr = (L.View * len(views))()
         for i, ((w, h, u), (rgba, dep)) in enumerate(zip(views, outputs)):
             arr[i].u = u
             arr[i].out = L.Image(rgba.data_ptr(), rgba.stride(0) * 4, dep.data_ptr() if dep is not None else None,
                                  dep.stride(0) * 4 if dep is not None else 0, w, h)
             arr[i].coverage_offset = 0.0
-        o = L.BatchOptions(warp_tile_w, tiles_per_grab, use_graph, schedule)
+        o = L.BatchOptions(warp_tile_w, tiles_per_grab, use_graph, schedule, density_format, surrogate)
         st = textures.scene() if isinstance(textures, Textures) else textures
         L.check(self.lib.mm_clouds_march_batch(self.ctx, arr, len(views), C.byref(st), C.byref(o), _stream_ptr(stream)),
                 "mm_clouds_march_batch")

@@ -89,3 +89,51 @@ def test_uneven_batch_and_autotune(cuda, env):
     print("  blocks %8.2f   graph %8.2f" % (table[20], table[21]))
     assert best.warp_tile_w in (4, 8, 16, 32) and 1 <= best.tiles_per_grab <= 16
     assert all(v > 0 for v in table)
+
+
+def test_batch_fp16_and_surrogate_equal_single_views(cuda, mmlib, env):
+    # config[4]'s batch: FP16 density and the learned sun cone, in the graph schedule.  FP16 views
+    # are the single-view launches themselves (identical bytes); surrogate views add their deferred
+    # terms with atomics, whose order differs from run to run (last-bit differences only).
+    import ctypes as C
+    import marshmallow as mm
+    import marshmallow.lib as L
+    from gpu_util import stream_ptr
+    tex, r = env
+    sp = stream_ptr(cuda)
+    per = 1 << 16
+    X = cuda.empty((2 * per, 16), dtype=cuda.bfloat16, device="cuda")
+    T = cuda.empty(2 * per, dtype=cuda.float32, device="cuda")
+    n = C.c_int()
+    assert mmlib.mm_surrogate_generate(1, 2, per, 150000.0, C.c_void_p(X.data_ptr()), C.c_void_p(T.data_ptr()),
+                                       C.byref(n), sp) == 0
+    net = C.c_void_p()
+    assert mmlib.mm_mlp_create(5, C.byref(net)) == 0
+    assert mmlib.mm_mlp_train(net, C.c_void_p(X.data_ptr()), C.c_void_p(T.data_ptr()), n.value, 16384, 32, 3e-3,
+                              None, sp) == 0
+    views = mm.scene.cubemap_views(96) + [(320, 180, mm.scene.uniforms(320, 180, yaw=40.0, pitch=20.0)),
+                                         (200, 120, mm.scene.uniforms(200, 120, sun_elevation=-8.0))]
+    night = mm.render.Textures.from_arrays({"night_sky": np.full((32, 64, 4), 90, np.uint8)})
+    tex.handles["night_sky"] = night.handles["night_sky"]
+    tex.set_density_format(L.FORMAT_FP16)
+    try:
+        for sur in (None, net.value):
+            outs = _outputs(cuda, views)
+            r.march_batch(views, tex, outs, density_format=L.FORMAT_FP16, surrogate=sur)
+            cuda.cuda.synchronize()
+            for (w, h, u), (rgba, dep) in zip(views, outs):
+                ref = cuda.zeros((h, w, 4), device="cuda")
+                rdep = cuda.zeros((h, w), device="cuda")
+                r.march(u, tex, ref, rdep, density_format=L.FORMAT_FP16, surrogate=sur)
+                cuda.cuda.synchronize()
+                a, b = rgba.cpu().numpy(), ref.cpu().numpy()
+                if sur is None:
+                    assert np.array_equal(a, b), (w, h)
+                else:
+                    assert np.allclose(a, b, rtol=1e-4, atol=1e-6), (w, h, float(np.abs(a - b).max()))
+                assert np.array_equal(dep.cpu().numpy(), rdep.cpu().numpy()), (w, h)
+    finally:
+        tex.set_density_format(L.FORMAT_UNORM8)
+        mmlib.mm_mlp_destroy(net)
+        del tex.handles["night_sky"]
+        night.close()

@@ -392,9 +392,19 @@ def measure_small_launches(renderer, textures, flush, stream):
     a = torch.zeros((256, 256, 4), device="cuda")
     d = torch.zeros((256, 256), device="cuda")
     ms256 = _median_ms(lambda: renderer.march(u0, textures, a, d), flush, stream, n=5, warm=2)
+    W4, H4 = 3840, 2160
+    rgba4 = torch.zeros((H4, W4, 4), device="cuda")
+    dep4 = torch.zeros((H4, W4), device="cuda")
+    per4 = []
+    for k in (0, 5, 10, 15):
+        u = mm.scene.sweep_uniforms(k, W4, H4)
+        u.sun.color[3] = float(k)
+        per4.append(_median_ms(lambda: renderer.march(u, textures, rgba4, dep4, pixel_mode=L.PIXELS_PHASE16), flush,
+                               stream, n=5, warm=2))
     return {"phase16_1080p": {"ms_mean": round(mean, 4), "ms_per_frame": [round(x, 4) for x in per],
                               "mrays_per_s": round((W // 4) * (H // 4) / mean / 1e3, 1),
                               "note": "march of the pixels of phase k of sweep frame k (1/16 of 1920x1080)"},
+            "phase16_4k": {"ms_mean": round(sum(per4) / len(per4), 4), "frames": [0, 5, 10, 15]},
             "camera_256_ms": round(ms256, 4)}
 
 

@@ -965,7 +965,10 @@ __device__ __forceinline__ int tile_py(int by, int warp, int lane) {
 #define MM_LATENCY_MIN_BLOCKS 3
 #endif
 
-constexpr long long kLatencyRays = 262144;
+#ifndef MM_LATENCY_RAYS
+#define MM_LATENCY_RAYS 262144
+#endif
+constexpr long long kLatencyRays = MM_LATENCY_RAYS;
 #ifndef MM_LATENCY_SCHEDULE
 #define MM_LATENCY_SCHEDULE 1  // launches of at most kLatencyRays rays: 1 = team march, 0 = one thread per ray
 #endif

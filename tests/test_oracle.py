@@ -550,3 +550,18 @@ def test_sphere_intersection_needs_no_fp64():
             assert (err / ts[np.float64]).max() < 5e-5
             assert err.max() < 0.5
             assert (err / ts[np.float64])[el < np.radians(1.0)].max() < 1e-5
+
+
+def test_texture_unit_filter_matches_recorded_hardware_fetches(orc, oracle_textures):
+    # tests/golden/texture_unit_fetches.npz: fetches of the GB300's texture unit (LINEAR, WRAP,
+    # normalized coordinates, UNORM8) recorded by tests/golden/make_texture_unit_golden.py on the
+    # seed-0 textures and two random ones (2D 53x37, 3D 24x20x12).  The oracle's texture-unit filter
+    # reproduces every channel of every fetch; the exact-weight filter does not.
+    g = np.load(os.path.join(GOLDEN, "texture_unit_fetches.npz"))
+    for name in ("weather", "curl", "low_res", "hi_res", "random_2d", "random_3d"):
+        texels = g[name + "_texels"] if name.startswith("random") else oracle_textures[name]
+        coords, want = g[name + "_coords"], g[name + "_fetched"]
+        got = orc.sample(texels, coords, filter=orc.FILTER_TEXTURE_UNIT)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), name
+        exact = orc.sample(texels, coords, filter=orc.FILTER_EXACT)
+        assert np.mean(np.any(exact != want, axis=1)) > 0.5, name

@@ -1049,6 +1049,12 @@ __global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_LATENCY_MIN_BLOCKS) ma
 #ifndef MM_TEAM_MIN_BLOCKS
 #define MM_TEAM_MIN_BLOCKS 4
 #endif
+// Cone taps a team member issues together (6 or 3).  1920x1080/16 sweep mean, 256x256: taps in
+// sixes at 4 blocks/SM (127 registers) 0.247 / 0.160 ms; in threes at 5 / 6 / 8 blocks/SM 0.256 /
+// 0.282 / 0.321 and 0.163 / 0.179 / 0.189; sixes at 5 blocks/SM (96 registers) 0.256 / 0.169.
+#ifndef MM_TEAM_CONE_GROUP
+#define MM_TEAM_CONE_GROUP 6
+#endif
 constexpr int kTeam = MM_TEAM_LANES;
 static_assert(kTeam == 4 || kTeam == 8, "team size");
 // Rays of a warp (32 / kTeam) as a 2x2 (teams of 8) or 4x2 (teams of 4) pixel tile; the four warps
@@ -1090,7 +1096,10 @@ __device__ __forceinline__ void team_ray(const MarchLaunch& p, const Frame& f, c
             if (!noHits && lo > 0.0f) {
                 hi = hires_finish<E>(hires_fetch<E, S>(p, curl_displace<E>(g, stepSize, cu)), g.rh, lo, nh);
                 if (hi >= 0.0001f) {
-                    const float dal = cone_taps<E, S, 6, true>(p, f, s_cone, 0, pos, stepSize, 0.0f, nt, nh);
+                    float dal = 0.0f;
+#pragma unroll
+                    for (int i = 0; i < 6; i += MM_TEAM_CONE_GROUP)
+                        dal = cone_taps<E, S, MM_TEAM_CONE_GROUP, true>(p, f, s_cone, i, pos, stepSize, dal, nt, nh);
                     y = shade_term<E>(dal, lo, g.rh, r.cosTheta, r.hg);
                 }
             }

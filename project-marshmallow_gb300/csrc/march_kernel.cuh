@@ -997,6 +997,205 @@ __device__ __forceinline__ void march_tiled_body(const MarchLaunch& p) {
     if (C) flush_work(p.counters, w);
 }
 
+// ------------------------------------------------------------------------------ deferred sun cones
+//
+// Full frames.  The sun cone of an accumulated sample (:441-453) changes only the light term
+// (`transmittance`, :462), never the march: the loop's path, `accum` and `firstT` depend on the
+// density alone.  So a lane that accumulates a sample appends a record of it -- t, step size, low-res
+// density, `accum` before the sample, its lane -- to its warp's FIFO pool in shared memory and marches
+// on.  Once the pool holds 32 records the warp computes the 32 oldest cones at once, one
+// record per lane, every lane taking part (helpers included: rays that have ended, rays below the
+// horizon, pixels outside the image).  Each lane writes its record's blend target
+// inScatter * HG * beers (:455-460) back into the pool, and each owner then blends its records of the
+// round into its transmittance in pool order, which is its accumulation order, with the sample's own
+// `accum` (:462).  Clouds are coherent, so 19 of 32 lanes on average accumulate in an iteration in
+// which any does (3840x2160 sweep frame 3, oracle trace): the inline cone runs with those lanes while
+// the rest wait, pooled records fill ~92% of the lanes.  A record's position and relative height are
+// recomputed from t and the owner's ray by the march's own expressions, and the owners' masks of a
+// round reuse the round's slots, so the pool takes 4.4 KB a block: the pooled kernel loses to the
+// inline cone when the pool's shared memory takes L1 from the texture cache (1920x1080 sweep: 1.071 ms
+// with 8 KB a block, 1.012 with 4.9 KB; inline 1.074).  Every sample, tap and blend is the shader's
+// arithmetic in its order per ray, so results and work counts equal the one-thread march bit for bit
+// in exact mode.
+constexpr int kPool = 64;  // records per warp: < 32 after a round, + at most 32 per iteration
+struct ConePool {
+    float t[MM_TILED_WARPS][kPool], step[MM_TILED_WARPS][kPool], acc[MM_TILED_WARPS][kPool];
+    union {
+        float lo;       // the record's low-res density
+        unsigned mask;  // during a round, at slot head + o: the round's lanes holding owner o's records
+    } lm[MM_TILED_WARPS][kPool];
+    unsigned char own[MM_TILED_WARPS][kPool];
+    int tail[MM_TILED_WARPS];  // records appended so far (slot = index mod kPool)
+};
+
+// One round: the `take` (<= 32) oldest records of the warp's pool, one per lane, then each owner's
+// blends in pool order.  Every lane of the warp calls it with the same head and take.
+template <bool E, int S>
+__device__ __forceinline__ void cone_round(const MarchLaunch& p, const Frame& f, const V3* cone, ConePool& q,
+                                           int head, int take, V3 rd, float& trans, float cosTheta, float hg,
+                                           Work& w) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    __syncwarp();  // the appended records are visible to the warp
+    const bool work = lane < take;
+    const int slot = (head + lane) & (kPool - 1);
+    const int o = work ? (int)q.own[wp][slot] : 32 + lane;  // idle lanes: a value no owner has
+    const int src = o & 31;
+    const float rx = __shfl_sync(full, rd.x, src), ry = __shfl_sync(full, rd.y, src);
+    const float rz = __shfl_sync(full, rd.z, src);
+    const float cosO = __shfl_sync(full, cosTheta, src), hgO = __shfl_sync(full, hg, src);
+    if (work) {
+        const float t = q.t[wp][slot], stepSize = q.step[wp][slot];
+        const V3 pos = f.cam + t * V3{rx, ry, rz};  // the march's own expressions for this sample
+        const float rh = geo_at<E>(f, pos).rh;
+        float dal = 0.0f;
+#pragma unroll 1
+        for (int i = 0; i < 6; ++i) dal = cone_taps<E, S, 1>(p, f, cone, i, pos, stepSize, dal, w.test, w.hires);
+        q.t[wp][slot] = shade_term<E>(dal, q.lm[wp][slot].lo, rh, cosO, hgO);
+    }
+    q.lm[wp][slot].mask = 0u;  // this lane's slot of the round: read above (if it held a record)
+    const unsigned same = __match_any_sync(full, o);
+    __syncwarp();
+    if (work && lane == __ffs(same) - 1) q.lm[wp][(head + o) & (kPool - 1)].mask = same;
+    __syncwarp();
+    unsigned mine = q.lm[wp][slot].mask;
+    while (mine) {  // :462, in accumulation order
+        const int sl = (head + __ffs(mine) - 1) & (kPool - 1);
+        mine &= mine - 1u;
+        trans = mixf(trans, q.t[wp][sl], 1.0f - q.acc[wp][sl]);
+    }
+    __syncwarp();  // the round's slots are read before later appends reuse them
+}
+
+// The march of pixel (px, py) with deferred sun cones (inside = false: no pixel, a helper lane).
+template <bool E, int S, bool SC>
+__device__ __forceinline__ void march_pixel_q(const MarchLaunch& p, const Frame& f, const V3* cone, ConePool& q,
+                                              int px, int py, bool inside, Work& w) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    Ray r{};
+    bool live = false;
+    if (inside) {
+        r = ray_setup<E, S>(p, f, px, py);
+        if (r.killed)
+            store_pixel(p, px, py, make_float4(r.bg.x, r.bg.y, r.bg.z, r.alpha), CUDART_INF_F);
+        else
+            live = true;
+    }
+    if (lane == 0) q.tail[wp] = 0;
+    float accum = 0.0f, trans = 1.0f;
+    float stepSize = 0.05f * f.thickness;  // :390
+    bool noHits = true;
+    int misses = 0, steps = 0, iterations = 0;
+    int head = 0;  // records of the warp's pool consumed so far (the same in every lane)
+    float firstT = CUDART_INF_F;
+    float t = r.t0;
+    bool alive = live && t < r.t1;  // :408, the loop condition on entry
+    __syncwarp();
+    for (;;) {
+        if (alive) {  // one iteration of :408-482
+            ++w.iter;
+            bool next = true;  // false: the loop ends here (no increment)
+            const V3 pos = f.cam + t * r.rd;
+            const Geo g = geo_at<E>(f, pos);
+            F4 cu;
+            if (SC && !noHits) cu = curl_fetch<E, S>(p, g);
+            float density = cloud_test<E, S>(p, f, g, w.test);
+            const float loDensity = density;
+            do {  // `break` = the shader's `continue`
+                if (density > 0.0f) {
+                    misses = 0;
+                    if (noHits) {  // :428-434
+                        t -= stepSize;
+                        stepSize *= 0.3f;
+                        noHits = false;
+                        break;
+                    }
+                    if (SC)
+                        density = hires_finish<E>(hires_fetch<E, S>(p, curl_displace<E>(g, stepSize, cu)), g.rh,
+                                                  density, w.hires);
+                    else
+                        density = cloud_hires<E, S>(p, g, stepSize, density, w.hires);
+                    if (density < 0.0001f) break;
+                    // the cone and blend of this sample (:441-462) come later; an owner's records
+                    // take increasing slots, so the pool keeps each ray's order
+                    const int slot = atomicAdd(&q.tail[wp], 1) & (kPool - 1);
+                    q.t[wp][slot] = t;
+                    q.step[wp][slot] = stepSize;
+                    q.lm[wp][slot].lo = loDensity;
+                    q.acc[wp][slot] = accum;
+                    q.own[wp][slot] = (unsigned char)lane;
+                    ++w.acc;
+                    if (firstT == CUDART_INF_F) firstT = t;
+                    accum += density;
+                } else if (!noHits) {  // :468-474
+                    misses++;
+                    if (misses >= 10) {
+                        noHits = true;
+                        stepSize = M<E>::div(stepSize, 0.3f);
+                    }
+                }
+                if (accum > 0.99f) {
+                    accum = 1.0f;
+                    next = false;
+                    break;
+                }
+                if (++steps > 100) next = false;
+            } while (false);
+            if (next) {
+                t += stepSize;
+                ++iterations;
+                alive = t < r.t1 && iterations < kMaxIterations;
+            } else {
+                alive = false;
+            }
+        }
+        __syncwarp();
+        if (q.tail[wp] - head >= 32) {  // < 64 records: < 32 after a round, at most 32 appended since
+            cone_round<E, S>(p, f, cone, q, head, 32, r.rd, trans, r.cosTheta, r.hg, w);
+            head += 32;
+        }
+        if (!__any_sync(full, alive)) break;
+    }
+    const int count = q.tail[wp] - head;
+    if (count > 0) cone_round<E, S>(p, f, cone, q, head, count, r.rd, trans, r.cosTheta, r.hg, w);
+    if (live) store_pixel(p, px, py, composite<E>(p.u, f, r.rd, r.bg, r.alpha, accum, trans), firstT);
+}
+
+template <bool E, int S, bool C, bool SC>
+__device__ __forceinline__ void march_tiled_q_body(const MarchLaunch& p) {
+    __shared__ V3 s_cone[6];
+    __shared__ ConePool s_q;
+    cone_offsets(p.u, s_cone);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int by = (int)blockIdx.y < p.row_split ? p.row_split - 1 - (int)blockIdx.y : (int)blockIdx.y;
+    const int tx = tile_px((int)blockIdx.x, warp, lane);
+    const int ty = tile_py(by, warp, lane);
+    int px = tx, py = ty;
+    if (p.pixel_mode == MM_PIXELS_PHASE16) {  // :292-298
+        px = tx * 4 + (p.phase % 4);
+        py = ty * 4 + (p.phase / 4);
+    }
+    const Frame f = make_frame<E>(p);
+    Work w;
+    march_pixel_q<E, S, SC>(p, f, s_cone, s_q, px, py, px < p.width && py < p.height, w);
+    if (C) flush_work(p.counters, w);
+}
+
+#ifndef MM_POOL_CARVEOUT_PCT
+#define MM_POOL_CARVEOUT_PCT 20  // carveout preference of the pooled kernel, percent (0: computed)
+#endif
+#ifndef MM_MARCH_CARVEOUT
+#define MM_MARCH_CARVEOUT 1  // pooled cones: request the smallest shared-memory carveout (the rest is L1)
+#endif
+#ifndef MM_CONE_POOL
+#define MM_CONE_POOL 1  // full frames: pooled cones where the pixel pitch is coarse (1), never (0), always (2)
+#endif
+#ifndef MM_CONE_POOL_PITCH
+#define MM_CONE_POOL_PITCH 6.5e-4f  // vertical pixel pitch 2 tan(fov/2) / height from which cones are pooled
+#endif
+
 #ifndef MM_LARGE_PAIR
 // Full frames: large steps in pairs with FP32 decisions (1) or one at a time (0).  Measured on the
 // 4K sweep: 3.367 ms in pairs against 3.240 one at a time (the lanes of a warp fall out of step).
@@ -1010,6 +1209,12 @@ template <bool E, int S, bool C>
 __global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_MARCH_MIN_BLOCKS) march_tiled_kernel(MarchLaunch p) {
     march_tiled_body<E, S, C, MM_CONE_GROUP, (MM_SPEC_CURL != 0), (MM_TILED_PARAM_CONE != 0),
                      (E || S != MM_SAMPLER_HARDWARE) ? 0 : MM_LARGE_PAIR>(p);
+}
+
+// Full frames with deferred, pooled sun cones (above).
+template <bool E, int S, bool C>
+__global__ void __launch_bounds__(MM_TILED_WARPS * 32, MM_MARCH_MIN_BLOCKS) march_tiled_pool_kernel(MarchLaunch p) {
+    march_tiled_q_body<E, S, C, (MM_SPEC_CURL != 0)>(p);
 }
 
 // Full frames with FP16 (or BF16) density textures under MM_MATH_FAST_HALF2: large-step decisions
@@ -1301,6 +1506,49 @@ inline int horizon_row_split(const MarchLaunch& p, int block_rows, int rows_per_
     return split;
 }
 
+// Pooled cones or each lane's own, per launch.  Pooling pays where the inline cone leaves more lanes
+// idle: neighbouring rays of a warp tile are less alike where a pixel spans a larger angle (oracle
+// trace, sweep frame 3: 15 of 32 lanes accumulate together at 1920x1080, 19 at 3840x2160), while the
+// pool's bookkeeping costs the same per iteration.  16-frame sweep, 60 degree field of view, inline
+// -> pooled: 1920x1080 1.074 -> 1.012 ms, 2560x1440 1.590 -> 1.576, 2880x1620 1.988 -> 1.973,
+// 3200x1800 2.394 -> 2.396, 3840x2160 3.240 -> 3.273.  Pooled from a vertical pitch of 6.5e-4
+// (2880x1620 at 60 degrees: 7.1e-4; 3840x2160: 5.3e-4).
+__host__ __forceinline__ bool use_cone_pool(const MarchLaunch& p) {
+    if (MM_CONE_POOL == 0) return false;
+    if (MM_CONE_POOL == 2) return true;
+    return 2.0f * p.u.camera.camera_params[1] >= MM_CONE_POOL_PITCH * p.uv_h;
+}
+
+// The pooled kernel's shared memory is small (4.4 KB a block), and the rest of the SM's unified L1 is
+// its texture cache.  Without a preference the driver gave it a 132 KB shared-memory carveout; the
+// preference computed from its need (10 blocks x (4.4 + 1 KB reserved) = 23% of 228 KB) still got
+// 100 KB, and 20% (or 12%) got 64 KB, which holds 11 blocks (6%: 32 KB, 5 blocks).  1920x1080, one
+// sweep frame: L1 hit rate 88% / 91.4% / 93.0% at 132 / 100 / 64 KB (the inline kernel: 93.0% at its
+// 32 KB); 16-frame sweep at 64 KB against 100 KB: 1920x1080 1.012 / 1.021 ms, 3840x2160 3.273 /
+// 3.295.  So 20% is requested once per device (MM_POOL_CARVEOUT_PCT = 0: the computed preference).
+// A hint only: a failure is cleared and ignored.
+template <bool E, int S, bool C>
+void pool_carveout() {
+    static unsigned done = 0;  // a bit per device; setting the attribute twice is harmless
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev >= 32 || (done >> dev & 1u)) {
+        cudaGetLastError();
+        return;
+    }
+    int per_sm = 0, reserved = 0;
+    cudaFuncAttributes a{};
+    if (cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) == cudaSuccess &&
+        cudaFuncGetAttributes(&a, march_tiled_pool_kernel<E, S, C>) == cudaSuccess && per_sm > 0) {
+        const long long need = (long long)MM_MARCH_MIN_BLOCKS * ((long long)a.sharedSizeBytes + reserved);
+        int pct = MM_POOL_CARVEOUT_PCT > 0 ? MM_POOL_CARVEOUT_PCT : (int)((100 * need + per_sm - 1) / per_sm);
+        pct = pct < 1 ? 1 : (pct > 100 ? 100 : pct);
+        cudaFuncSetAttribute(march_tiled_pool_kernel<E, S, C>, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+    }
+    cudaGetLastError();
+    done |= 1u << dev;
+}
+
 template <bool E, int S>
 int launch_tiled(const MarchLaunch& p0, cudaStream_t s, bool half2 = false) {
     MarchLaunch p = p0;
@@ -1333,6 +1581,14 @@ int launch_tiled(const MarchLaunch& p0, cudaStream_t s, bool half2 = false) {
             march_tiled_h2_kernel<true><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
         else
             march_tiled_h2_kernel<false><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
+    } else if (use_cone_pool(p)) {
+        if (p.counters) {
+            if (MM_MARCH_CARVEOUT) pool_carveout<E, S, true>();
+            march_tiled_pool_kernel<E, S, true><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
+        } else {
+            if (MM_MARCH_CARVEOUT) pool_carveout<E, S, false>();
+            march_tiled_pool_kernel<E, S, false><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
+        }
     } else if (p.counters) {
         march_tiled_kernel<E, S, true><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
     } else {

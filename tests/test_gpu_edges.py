@@ -170,13 +170,16 @@ def test_half2_coverage_test_needs_fp16_density(cuda, mmlib, env):
 
 
 def test_kernel_variants_exact(cuda, orc, oracle_textures, env):
-    # The march picks one of three kernels per launch (full frames, launches of <= 262144 rays,
-    # larger 1/16-pixel launches); all three are the same arithmetic and equal the oracle bit for bit.
+    # The march picks its kernel per launch (full frames with pooled or inline sun cones by the pixel
+    # pitch, launches of <= 262144 rays, larger 1/16-pixel launches); all are the same arithmetic and
+    # equal the oracle bit for bit.  2880x1620 at 60 degrees pools its cones, 1280x720 at 20 degrees
+    # (pitch 2 tan(10 deg) / 720 = 4.9e-4) does not.
     import marshmallow as mm
     import marshmallow.lib as L
     tex, r = env
-    for (w, h, mode) in [(2880, 1620, 1), (640, 400, 0), (640, 400, 1)]:
-        u = mm.scene.uniforms(w, h, yaw=30.0, pitch=10.0, time=1.0)
+    for (w, h, mode, fov) in [(2880, 1620, 1, 60.0), (2880, 1620, 0, 60.0), (1280, 720, 0, 20.0), (640, 400, 0, 60.0),
+                              (640, 400, 1, 60.0)]:
+        u = mm.scene.uniforms(w, h, yaw=30.0, pitch=10.0, fov=fov, time=1.0)
         u.sun.color[3] = 9.0
         rgba = cuda.zeros((h, w, 4), device="cuda")
         dep = cuda.zeros((h, w), device="cuda")

@@ -372,6 +372,8 @@ int mm_context_create(mm_context* out) {
     if (!c) return fail(MM_ERR_OUT_OF_MEMORY, "context: host allocation failed");
     c->device = dev;
     cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, dev);
+    mm::prepare_march_fast();
+    mm::prepare_march_exact();
     cudaError_t e = cudaMalloc(&c->d_work, 64 * sizeof(unsigned int));
     if (e != cudaSuccess) {
         delete c;

@@ -5,6 +5,8 @@
 
 namespace mm {
 
+void prepare_march_exact() { march::prepare_march_kernels<true>(); }
+
 int launch_march_exact(const MarchLaunch& p, int sampler, int schedule, unsigned int* work, int num_sms,
                        cudaStream_t s) {
     if (schedule == MM_SCHEDULE_TILED) {

@@ -4,6 +4,8 @@
 
 namespace mm {
 
+void prepare_march_fast() { march::prepare_march_kernels<false>(); }
+
 int launch_march_fast(const MarchLaunch& p, int sampler, int format, int schedule, int half2, unsigned int* work,
                       int num_sms, cudaStream_t s) {
     (void)format;

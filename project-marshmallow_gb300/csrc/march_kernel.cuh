@@ -1003,8 +1003,8 @@ __device__ __forceinline__ void march_tiled_body(const MarchLaunch& p) {
 // (`transmittance`, :462), never the march: the loop's path, `accum` and `firstT` depend on the
 // density alone.  So a lane that accumulates a sample appends a record of it -- t, step size, low-res
 // density, `accum` before the sample, its lane -- to its warp's FIFO pool in shared memory and marches
-// on.  Once the pool holds 32 records the warp computes the 32 oldest cones at once, one
-// record per lane, every lane taking part (helpers included: rays that have ended, rays below the
+// on.  Once the pool holds 32 records (one warp reduction per iteration counts the appends and the
+// rays still marching) the warp computes the 32 oldest cones at once, one record per lane, every lane taking part (helpers included: rays that have ended, rays below the
 // horizon, pixels outside the image).  Each lane writes its record's blend target
 // inScatter * HG * beers (:455-460) back into the pool, and each owner then blends its records of the
 // round into its transmittance in pool order, which is its accumulation order, with the sample's own
@@ -1087,12 +1087,13 @@ __device__ __forceinline__ void march_pixel_q(const MarchLaunch& p, const Frame&
     float stepSize = 0.05f * f.thickness;  // :390
     bool noHits = true;
     int misses = 0, steps = 0, iterations = 0;
-    int head = 0;  // records of the warp's pool consumed so far (the same in every lane)
+    int head = 0, pending = 0;  // records of the warp's pool consumed / waiting (the same in every lane)
     float firstT = CUDART_INF_F;
     float t = r.t0;
     bool alive = live && t < r.t1;  // :408, the loop condition on entry
     __syncwarp();
     for (;;) {
+        bool pushed = false;
         if (alive) {  // one iteration of :408-482
             ++w.iter;
             bool next = true;  // false: the loop ends here (no increment)
@@ -1125,6 +1126,7 @@ __device__ __forceinline__ void march_pixel_q(const MarchLaunch& p, const Frame&
                     q.lm[wp][slot].lo = loDensity;
                     q.acc[wp][slot] = accum;
                     q.own[wp][slot] = (unsigned char)lane;
+                    pushed = true;
                     ++w.acc;
                     if (firstT == CUDART_INF_F) firstT = t;
                     accum += density;
@@ -1150,15 +1152,17 @@ __device__ __forceinline__ void march_pixel_q(const MarchLaunch& p, const Frame&
                 alive = false;
             }
         }
-        __syncwarp();
-        if (q.tail[wp] - head >= 32) {  // < 64 records: < 32 after a round, at most 32 appended since
+        // one reduction gives the records appended (low 6 bits) and the rays still marching (x 64)
+        const unsigned sum = __reduce_add_sync(full, (pushed ? 1u : 0u) + (alive ? 64u : 0u));
+        pending += (int)(sum & 63u);
+        if (pending >= 32) {  // < 64 records: < 32 after a round, at most 32 appended since
             cone_round<E, S>(p, f, cone, q, head, 32, r.rd, trans, r.cosTheta, r.hg, w);
             head += 32;
+            pending -= 32;
         }
-        if (!__any_sync(full, alive)) break;
+        if (sum < 64u) break;
     }
-    const int count = q.tail[wp] - head;
-    if (count > 0) cone_round<E, S>(p, f, cone, q, head, count, r.rd, trans, r.cosTheta, r.hg, w);
+    if (pending > 0) cone_round<E, S>(p, f, cone, q, head, pending, r.rd, trans, r.cosTheta, r.hg, w);
     if (live) store_pixel(p, px, py, composite<E>(p.u, f, r.rd, r.bg, r.alpha, accum, trans), firstT);
 }
 
@@ -1190,10 +1194,7 @@ __device__ __forceinline__ void march_tiled_q_body(const MarchLaunch& p) {
 #define MM_MARCH_CARVEOUT 1  // pooled cones: request the smallest shared-memory carveout (the rest is L1)
 #endif
 #ifndef MM_CONE_POOL
-#define MM_CONE_POOL 1  // full frames: pooled cones where the pixel pitch is coarse (1), never (0), always (2)
-#endif
-#ifndef MM_CONE_POOL_PITCH
-#define MM_CONE_POOL_PITCH 6.5e-4f  // vertical pixel pitch 2 tan(fov/2) / height from which cones are pooled
+#define MM_CONE_POOL 1  // full frames: sun cones pooled per warp (1) or each lane's inline cone (0)
 #endif
 
 #ifndef MM_LARGE_PAIR
@@ -1506,18 +1507,12 @@ inline int horizon_row_split(const MarchLaunch& p, int block_rows, int rows_per_
     return split;
 }
 
-// Pooled cones or each lane's own, per launch.  Pooling pays where the inline cone leaves more lanes
-// idle: neighbouring rays of a warp tile are less alike where a pixel spans a larger angle (oracle
-// trace, sweep frame 3: 15 of 32 lanes accumulate together at 1920x1080, 19 at 3840x2160), while the
-// pool's bookkeeping costs the same per iteration.  16-frame sweep, 60 degree field of view, inline
-// -> pooled: 1920x1080 1.074 -> 1.012 ms, 2560x1440 1.590 -> 1.576, 2880x1620 1.988 -> 1.973,
-// 3200x1800 2.394 -> 2.396, 3840x2160 3.240 -> 3.273.  Pooled from a vertical pitch of 6.5e-4
-// (2880x1620 at 60 degrees: 7.1e-4; 3840x2160: 5.3e-4).
-__host__ __forceinline__ bool use_cone_pool(const MarchLaunch& p) {
-    if (MM_CONE_POOL == 0) return false;
-    if (MM_CONE_POOL == 2) return true;
-    return 2.0f * p.u.camera.camera_params[1] >= MM_CONE_POOL_PITCH * p.uv_h;
-}
+// Pooled cones or each lane's own (MM_CONE_POOL).  The pool pays more where the inline cone leaves more
+// lanes idle: neighbouring rays of a warp tile are less alike where a pixel spans a larger angle
+// (oracle trace, sweep frame 3: 15 of 32 lanes accumulate together at 1920x1080, 19 at 3840x2160).
+// 16-frame sweep, 60 degree field of view, inline -> pooled: 1920x1080 1.074 -> 0.993 ms, 2880x1620
+// 1.988 -> 1.924, 3200x1800 2.394 -> 2.338, 3840x2160 3.240 -> 3.212.
+__host__ __forceinline__ bool use_cone_pool(const MarchLaunch&) { return MM_CONE_POOL != 0; }
 
 // The pooled kernel's shared memory is small (4.4 KB a block), and the rest of the SM's unified L1 is
 // its texture cache.  Without a preference the driver gave it a 132 KB shared-memory carveout; the
@@ -1525,13 +1520,13 @@ __host__ __forceinline__ bool use_cone_pool(const MarchLaunch& p) {
 // 100 KB, and 20% (or 12%) got 64 KB, which holds 11 blocks (6%: 32 KB, 5 blocks).  1920x1080, one
 // sweep frame: L1 hit rate 88% / 91.4% / 93.0% at 132 / 100 / 64 KB (the inline kernel: 93.0% at its
 // 32 KB); 16-frame sweep at 64 KB against 100 KB: 1920x1080 1.012 / 1.021 ms, 3840x2160 3.273 /
-// 3.295.  So 20% is requested once per device (MM_POOL_CARVEOUT_PCT = 0: the computed preference).
-// A hint only: a failure is cleared and ignored.
+// 3.295.  So 20% is requested (MM_POOL_CARVEOUT_PCT = 0: the computed preference) when a context is
+// created, outside any stream capture.  A hint only: a failure is cleared and ignored.
 template <bool E, int S, bool C>
 void pool_carveout() {
-    static unsigned done = 0;  // a bit per device; setting the attribute twice is harmless
+    if (!MM_MARCH_CARVEOUT) return;
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev >= 32 || (done >> dev & 1u)) {
+    if (cudaGetDevice(&dev) != cudaSuccess) {
         cudaGetLastError();
         return;
     }
@@ -1546,7 +1541,15 @@ void pool_carveout() {
         cudaFuncSetAttribute(march_tiled_pool_kernel<E, S, C>, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
     }
     cudaGetLastError();
-    done |= 1u << dev;
+}
+
+// Kernel attributes of this arithmetic's march kernels for the current device.
+template <bool E>
+void prepare_march_kernels() {
+    pool_carveout<E, MM_SAMPLER_HARDWARE, false>();
+    pool_carveout<E, MM_SAMPLER_HARDWARE, true>();
+    pool_carveout<E, MM_SAMPLER_SOFTWARE, false>();
+    pool_carveout<E, MM_SAMPLER_SOFTWARE, true>();
 }
 
 template <bool E, int S>
@@ -1582,13 +1585,10 @@ int launch_tiled(const MarchLaunch& p0, cudaStream_t s, bool half2 = false) {
         else
             march_tiled_h2_kernel<false><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
     } else if (use_cone_pool(p)) {
-        if (p.counters) {
-            if (MM_MARCH_CARVEOUT) pool_carveout<E, S, true>();
+        if (p.counters)
             march_tiled_pool_kernel<E, S, true><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
-        } else {
-            if (MM_MARCH_CARVEOUT) pool_carveout<E, S, false>();
+        else
             march_tiled_pool_kernel<E, S, false><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
-        }
     } else if (p.counters) {
         march_tiled_kernel<E, S, true><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
     } else {

@@ -99,6 +99,10 @@ struct MarchLaunch {
 };
 
 // Kernel launchers (one translation unit per arithmetic mode).
+// Kernel attributes of the march kernels (the pooled kernels' shared-memory carveout) for the current
+// device; called when a context is created, outside any stream capture.
+void prepare_march_fast();
+void prepare_march_exact();
 int launch_march_exact(const MarchLaunch& p, int sampler, int schedule, unsigned int* work, int num_sms,
                        cudaStream_t s);
 int launch_march_fast(const MarchLaunch& p, int sampler, int format, int schedule, int half2, unsigned int* work,

@@ -170,10 +170,9 @@ def test_half2_coverage_test_needs_fp16_density(cuda, mmlib, env):
 
 
 def test_kernel_variants_exact(cuda, orc, oracle_textures, env):
-    # The march picks its kernel per launch (full frames with pooled or inline sun cones by the pixel
-    # pitch, launches of <= 262144 rays, larger 1/16-pixel launches); all are the same arithmetic and
-    # equal the oracle bit for bit.  2880x1620 at 60 degrees pools its cones, 1280x720 at 20 degrees
-    # (pitch 2 tan(10 deg) / 720 = 4.9e-4) does not.
+    # The march picks its kernel per launch (full frames with pooled sun cones, launches of <= 262144
+    # rays, larger 1/16-pixel launches); all are the same arithmetic and equal the oracle bit for bit.
+    # Full frames at two pixel pitches: 2880x1620 at 60 degrees, 1280x720 at 20 degrees.
     import marshmallow as mm
     import marshmallow.lib as L
     tex, r = env

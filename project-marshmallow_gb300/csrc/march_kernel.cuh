@@ -1018,6 +1018,17 @@ __device__ __forceinline__ void march_tiled_body(const MarchLaunch& p) {
 // arithmetic in its order per ray, so results and work counts equal the one-thread march bit for bit
 // in exact mode.
 constexpr int kPool = 64;  // records per warp: < 32 after a round, + at most 32 per iteration
+// Cone taps a lane of a round issues together (1, 2, 3 or 6).  3840x2160 / 1920x1080 sweeps: one at
+// a time 3.215 / 0.992 ms; in pairs 3.347 / 1.036 (spills at 48 registers), 3.328 / 1.025 at 9 blocks
+// per SM; in threes 3.819 / 1.186.
+#ifndef MM_POOL_CONE_GROUP
+#define MM_POOL_CONE_GROUP 1
+#endif
+// 1/16-pixel launches above kLatencyRays rays: pooled cones (1) or the inline kernel with cone taps in
+// threes at 6 blocks per SM (0).  3840x2160 at 1/16, sweep frames 0/5/10/15: 0.361 against 0.412 ms.
+#ifndef MM_PHASE16_POOL
+#define MM_PHASE16_POOL 1
+#endif
 struct ConePool {
     float t[MM_TILED_WARPS][kPool], step[MM_TILED_WARPS][kPool], acc[MM_TILED_WARPS][kPool];
     union {
@@ -1050,7 +1061,8 @@ __device__ __forceinline__ void cone_round(const MarchLaunch& p, const Frame& f,
         const float rh = geo_at<E>(f, pos).rh;
         float dal = 0.0f;
 #pragma unroll 1
-        for (int i = 0; i < 6; ++i) dal = cone_taps<E, S, 1>(p, f, cone, i, pos, stepSize, dal, w.test, w.hires);
+        for (int i = 0; i < 6; i += MM_POOL_CONE_GROUP)
+            dal = cone_taps<E, S, MM_POOL_CONE_GROUP>(p, f, cone, i, pos, stepSize, dal, w.test, w.hires);
         q.t[wp][slot] = shade_term<E>(dal, q.lm[wp][slot].lo, rh, cosO, hgO);
     }
     q.lm[wp][slot].mask = 0u;  // this lane's slot of the round: read above (if it held a record)
@@ -1574,6 +1586,11 @@ int launch_tiled(const MarchLaunch& p0, cudaStream_t s, bool half2 = false) {
             march_tiled_latency_kernel<E, S, true><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
         else
             march_tiled_latency_kernel<E, S, false><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
+    } else if (p.pixel_mode == MM_PIXELS_PHASE16 && MM_PHASE16_POOL) {
+        if (p.counters)
+            march_tiled_pool_kernel<E, S, true><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
+        else
+            march_tiled_pool_kernel<E, S, false><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
     } else if (p.pixel_mode == MM_PIXELS_PHASE16) {
         if (p.counters)
             march_tiled_phase16_kernel<E, S, true><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);

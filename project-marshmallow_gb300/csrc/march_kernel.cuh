@@ -1029,6 +1029,12 @@ constexpr int kPool = 64;  // records per warp: < 32 after a round, + at most 32
 #ifndef MM_PHASE16_POOL
 #define MM_PHASE16_POOL 1
 #endif
+// The team march's one-thread rows: pooled cones (1) or inline cone taps in threes (0).  1920x1080 at
+// 1/16, sweep mean: 0.256 ms pooled against 0.247 (the launch is bound by its longest rays, which the
+// teams march; the pool's rounds only add latency to the others).
+#ifndef MM_HYBRID_POOL
+#define MM_HYBRID_POOL 0
+#endif
 struct ConePool {
     float t[MM_TILED_WARPS][kPool], step[MM_TILED_WARPS][kPool], acc[MM_TILED_WARPS][kPool];
     union {
@@ -1400,6 +1406,9 @@ struct HybridGrid {
 template <bool E, int S, bool C>
 __global__ void __launch_bounds__(128, MM_TEAM_MIN_BLOCKS) march_hybrid_kernel(MarchLaunch p, HybridGrid hg) {
     __shared__ V3 s_cone[6];
+#if MM_HYBRID_POOL
+    __shared__ ConePool s_q;
+#endif
     cone_offsets(p.u, s_cone);
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1425,7 +1434,17 @@ __global__ void __launch_bounds__(128, MM_TEAM_MIN_BLOCKS) march_hybrid_kernel(M
         px = tx;
         py = ty;
     }
-    if (px >= p.width || py >= p.height) return;  // a team leaves together: its lanes share (px, py)
+    const bool inside = px < p.width && py < p.height;
+#if MM_HYBRID_POOL
+    if (!team_block) {  // every lane of the warp stays: the pool's rounds need them all
+        const Frame f = make_frame<E>(p);
+        Work w;
+        march_pixel_q<E, S, (MM_SPEC_CURL != 0)>(p, f, s_cone, s_q, px, py, inside, w);
+        if (C) flush_work(p.counters, w);
+        return;
+    }
+#endif
+    if (!inside) return;  // a team leaves together: its lanes share (px, py)
     const Frame f = make_frame<E>(p);
     if (team_block) {
         const int team = lane / kTeam, base = team * kTeam;

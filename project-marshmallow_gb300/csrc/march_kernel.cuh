@@ -1003,18 +1003,19 @@ __device__ __forceinline__ void march_tiled_body(const MarchLaunch& p) {
 // (`transmittance`, :462), never the march: the loop's path, `accum` and `firstT` depend on the
 // density alone.  So a lane that accumulates a sample appends a record of it -- t, step size, low-res
 // density, `accum` before the sample, its lane -- to its warp's FIFO pool in shared memory and marches
-// on.  Once the pool holds 32 records (one warp reduction per iteration counts the appends and the
-// rays still marching) the warp computes the 32 oldest cones at once, one record per lane, every lane taking part (helpers included: rays that have ended, rays below the
-// horizon, pixels outside the image).  Each lane writes its record's blend target
-// inScatter * HG * beers (:455-460) back into the pool, and each owner then blends its records of the
-// round into its transmittance in pool order, which is its accumulation order, with the sample's own
-// `accum` (:462).  Clouds are coherent, so 19 of 32 lanes on average accumulate in an iteration in
-// which any does (3840x2160 sweep frame 3, oracle trace): the inline cone runs with those lanes while
-// the rest wait, pooled records fill ~92% of the lanes.  A record's position and relative height are
-// recomputed from t and the owner's ray by the march's own expressions, and the owners' masks of a
-// round reuse the round's slots, so the pool takes 4.4 KB a block: the pooled kernel loses to the
-// inline cone when the pool's shared memory takes L1 from the texture cache (1920x1080 sweep: 1.071 ms
-// with 8 KB a block, 1.012 with 4.9 KB; inline 1.074).  Every sample, tap and blend is the shader's
+// on.  One warp reduction per iteration counts the appends and the rays still marching; once the pool
+// holds 32 records the warp computes the 32 oldest cones at once, one record per lane, every lane
+// taking part (helpers included: rays that have ended, rays below the horizon, pixels outside the
+// image).  Each lane writes its record's blend target inScatter * HG * beers (:455-460) back into the
+// pool, and each owner then blends its records of the round into its transmittance in pool order,
+// which is its accumulation order, with the sample's own `accum` (:462).  Clouds are coherent, so 19
+// of 32 lanes on average accumulate in an iteration in which any does (3840x2160 sweep frame 3, oracle
+// trace): the inline cone runs with those lanes while the rest wait; pooled records fill ~92% of the
+// lanes.  A record's position and relative height are recomputed from t and the owner's ray by the
+// march's own expressions, and the owners' masks of a round reuse the round's slots, so the pool takes
+// 4.4 KB a block.  Shared memory is taken from the L1 that caches the textures: with 28-byte records
+// (8 KB a block) the 1920x1080 sweep took 1.071 ms, with these 1.012 (inline cone: 1.074; both before
+// the per-iteration count became one reduction).  Every sample, tap and blend is the shader's
 // arithmetic in its order per ray, so results and work counts equal the one-thread march bit for bit
 // in exact mode.
 constexpr int kPool = 64;  // records per warp: < 32 after a round, + at most 32 per iteration

@@ -232,12 +232,15 @@ def test_night_branch(cuda, orc, renderer, gpu_textures, host_textures):
     handles = dict(gpu_textures.handles)
     handles["night_sky"] = nt.handles["night_sky"]
     tex = mm.render.Textures(handles=handles)
-    u = mm.scene.uniforms(96, 64, sun_elevation=-12.0)
-    rgba, dep = render(cuda, renderer, u, tex, 96, 64, sampler=L.SAMPLER_SOFTWARE, math=L.MATH_EXACT)
     h = dict(host_textures)
     h["night_sky"] = night
-    ref, rdep, _ = orc.march(u, h, 96, 64, precision=32)
-    assert np.array_equal(rgba, ref)
+    # 96x64: the team march; 720x400 (288,000 rays): the full-frame kernel with pooled sun cones
+    for w, hh in ((96, 64), (720, 400)):
+        u = mm.scene.uniforms(w, hh, sun_elevation=-12.0)
+        rgba, dep = render(cuda, renderer, u, tex, w, hh, sampler=L.SAMPLER_SOFTWARE, math=L.MATH_EXACT)
+        ref, rdep, _ = orc.march(u, h, w, hh, precision=32)
+        assert np.array_equal(rgba, ref), (w, hh)
+        assert np.array_equal(dep.view(np.uint32), rdep.view(np.uint32)), (w, hh)
     nt.close()
 
 

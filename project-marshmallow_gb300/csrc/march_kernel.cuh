@@ -1544,7 +1544,6 @@ inline int horizon_row_split(const MarchLaunch& p, int block_rows, int rows_per_
 // (oracle trace, sweep frame 3: 15 of 32 lanes accumulate together at 1920x1080, 19 at 3840x2160).
 // 16-frame sweep, 60 degree field of view, inline -> pooled: 1920x1080 1.074 -> 0.993 ms, 2880x1620
 // 1.988 -> 1.924, 3200x1800 2.394 -> 2.338, 3840x2160 3.240 -> 3.212.
-__host__ __forceinline__ bool use_cone_pool(const MarchLaunch&) { return MM_CONE_POOL != 0; }
 
 // The pooled kernel's shared memory is small (4.4 KB a block), and the rest of the SM's unified L1 is
 // its texture cache.  Without a preference the driver gave it a 132 KB shared-memory carveout; the
@@ -1594,42 +1593,50 @@ int launch_tiled(const MarchLaunch& p0, cudaStream_t s, bool half2 = false) {
     }
     dim3 grid((gw + kBlockTileW - 1) / kBlockTileW, (gh + kBlockTileH - 1) / kBlockTileH);
     p.row_split = horizon_row_split(p, (int)grid.y);
-    if ((long long)gw * gh <= kLatencyRays && MM_LATENCY_SCHEDULE == 1) {
-        const HybridGrid hg = hybrid_grid(p, gw, gh);
-        const int blocks = hg.team_blocks + hg.single_bx * (hg.rows_above + ((gh + 7) / 8 * 8 - hg.band1) / 8);
-        if (p.counters)
-            march_hybrid_kernel<E, S, true><<<blocks, 128, 0, s>>>(p, hg);
+    // Kernels that the build knobs leave unused are not instantiated (if constexpr).
+    const bool C = p.counters != nullptr;
+    const dim3 block(MM_TILED_WARPS * 32);
+    if ((long long)gw * gh <= kLatencyRays) {
+        if constexpr (MM_LATENCY_SCHEDULE == 1) {
+            const HybridGrid hg = hybrid_grid(p, gw, gh);
+            const int blocks =
+                hg.team_blocks + hg.single_bx * (hg.rows_above + ((gh + 7) / 8 * 8 - hg.band1) / 8);
+            if (C)
+                march_hybrid_kernel<E, S, true><<<blocks, 128, 0, s>>>(p, hg);
+            else
+                march_hybrid_kernel<E, S, false><<<blocks, 128, 0, s>>>(p, hg);
+        } else {
+            if (C)
+                march_tiled_latency_kernel<E, S, true><<<grid, block, 0, s>>>(p);
+            else
+                march_tiled_latency_kernel<E, S, false><<<grid, block, 0, s>>>(p);
+        }
+    } else if (p.pixel_mode == MM_PIXELS_PHASE16 && !MM_PHASE16_POOL) {
+        if constexpr (!MM_PHASE16_POOL) {
+            if (C)
+                march_tiled_phase16_kernel<E, S, true><<<grid, block, 0, s>>>(p);
+            else
+                march_tiled_phase16_kernel<E, S, false><<<grid, block, 0, s>>>(p);
+        }
+    } else if (!E && S == MM_SAMPLER_HARDWARE && half2 && p.pixel_mode != MM_PIXELS_PHASE16) {
+        if constexpr (!E && S == MM_SAMPLER_HARDWARE) {
+            if (C)
+                march_tiled_h2_kernel<true><<<grid, block, 0, s>>>(p);
+            else
+                march_tiled_h2_kernel<false><<<grid, block, 0, s>>>(p);
+        }
+    } else if (MM_CONE_POOL != 0 || p.pixel_mode == MM_PIXELS_PHASE16) {
+        if (C)
+            march_tiled_pool_kernel<E, S, true><<<grid, block, 0, s>>>(p);
         else
-            march_hybrid_kernel<E, S, false><<<blocks, 128, 0, s>>>(p, hg);
-    } else if ((long long)gw * gh <= kLatencyRays) {
-        if (p.counters)
-            march_tiled_latency_kernel<E, S, true><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
-        else
-            march_tiled_latency_kernel<E, S, false><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
-    } else if (p.pixel_mode == MM_PIXELS_PHASE16 && MM_PHASE16_POOL) {
-        if (p.counters)
-            march_tiled_pool_kernel<E, S, true><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
-        else
-            march_tiled_pool_kernel<E, S, false><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
-    } else if (p.pixel_mode == MM_PIXELS_PHASE16) {
-        if (p.counters)
-            march_tiled_phase16_kernel<E, S, true><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
-        else
-            march_tiled_phase16_kernel<E, S, false><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
-    } else if (!E && S == MM_SAMPLER_HARDWARE && half2) {
-        if (p.counters)
-            march_tiled_h2_kernel<true><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
-        else
-            march_tiled_h2_kernel<false><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
-    } else if (use_cone_pool(p)) {
-        if (p.counters)
-            march_tiled_pool_kernel<E, S, true><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
-        else
-            march_tiled_pool_kernel<E, S, false><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
-    } else if (p.counters) {
-        march_tiled_kernel<E, S, true><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
+            march_tiled_pool_kernel<E, S, false><<<grid, block, 0, s>>>(p);
     } else {
-        march_tiled_kernel<E, S, false><<<grid, MM_TILED_WARPS * 32, 0, s>>>(p);
+        if constexpr (MM_CONE_POOL == 0) {
+            if (C)
+                march_tiled_kernel<E, S, true><<<grid, block, 0, s>>>(p);
+            else
+                march_tiled_kernel<E, S, false><<<grid, block, 0, s>>>(p);
+        }
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "march_tiled_kernel launch");

@@ -103,6 +103,9 @@ struct MarchLaunch {
 // device; called when a context is created, outside any stream capture.
 void prepare_march_fast();
 void prepare_march_exact();
+void prepare_march_exact_sw();
+// The exact march with the software sampler (march_exact_sw.cu); launch_march_exact forwards to it.
+int launch_march_exact_sw(const MarchLaunch& p, int schedule, unsigned int* work, int num_sms, cudaStream_t s);
 int launch_march_exact(const MarchLaunch& p, int sampler, int schedule, unsigned int* work, int num_sms,
                        cudaStream_t s);
 int launch_march_fast(const MarchLaunch& p, int sampler, int format, int schedule, int half2, unsigned int* work,

@@ -21,12 +21,12 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
                       "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", os.path.join(REPO, "include")]
 # Units whose results must equal the CPU oracle bit for bit: no FMA contraction.
-EXACT_UNITS = {"march_exact.cu", "noise.cu", "reproject.cu", "shadow_exact.cu", "post_exact.cu"}
+EXACT_UNITS = {"march_exact.cu", "march_exact_sw.cu", "noise.cu", "reproject.cu", "shadow_exact.cu", "post_exact.cu"}
 # Production-arithmetic units (gated against the FP64 oracle, not bit-exact): FP32 denormals are
 # flushed to zero, which drops the denormal handling around the SFU operations (rsqrt, rcp, ex2,
 # lg2) from the march's dependent chains.
 FAST_UNITS = {"march_fast.cu", "surrogate.cu", "batch.cu", "reproject_fast.cu", "shadow.cu", "post.cu"}
-CUDA_UNITS = ["api.cu", "march_fast.cu", "march_exact.cu", "noise.cu", "peaks.cu", "noalloc.cu", "mlp.cu", "surrogate.cu", "batch.cu", "reproject.cu", "reproject_fast.cu", "shadow.cu", "shadow_exact.cu", "post.cu", "post_exact.cu"]
+CUDA_UNITS = ["api.cu", "march_fast.cu", "march_exact.cu", "march_exact_sw.cu", "noise.cu", "peaks.cu", "noalloc.cu", "mlp.cu", "surrogate.cu", "batch.cu", "reproject.cu", "reproject_fast.cu", "shadow.cu", "shadow_exact.cu", "post.cu", "post_exact.cu"]
 CXX_UNITS = ["scene.cpp", "assets.cpp"]
 HEADERS = ["mm_internal.h", "mm_math.h", "march_kernel.cuh", "tc.cuh", "shadow_kernel.cuh", "post_kernel.cuh"]
 

@@ -182,11 +182,14 @@ def test_kernel_variants_exact(cuda, orc, oracle_textures, env):
         u.sun.color[3] = 9.0
         rgba = cuda.zeros((h, w, 4), device="cuda")
         dep = cuda.zeros((h, w), device="cuda")
-        r.march(u, tex, rgba, dep, pixel_mode=mode, math=L.MATH_EXACT, sampler=L.SAMPLER_SOFTWARE)
+        cnt = cuda.zeros(4, dtype=cuda.int64, device="cuda")
+        r.march(u, tex, rgba, dep, pixel_mode=mode, math=L.MATH_EXACT, sampler=L.SAMPLER_SOFTWARE, counters=cnt)
         cuda.cuda.synchronize()
-        want, wd, _ = orc.march(u, oracle_textures, w, h, pixel_mode=mode)
+        want, wd, wc = orc.march(u, oracle_textures, w, h, pixel_mode=mode)
         got, gd = rgba.cpu().numpy(), dep.cpu().numpy()
         if mode:
             got, gd, want, wd = got[2::4, 1::4], gd[2::4, 1::4], want[2::4, 1::4], wd[2::4, 1::4]
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (w, h, mode)
         assert np.array_equal(gd.view(np.uint32), wd.view(np.uint32)), (w, h, mode)
+        # work counts (cloudTest, cloudHiRes, iterations, accumulated samples) equal the oracle's
+        assert np.array_equal(cnt.cpu().numpy().astype(np.uint64), wc), (w, h, mode, cnt.cpu().numpy(), wc)

@@ -503,7 +503,7 @@ def train_surrogate(lib, stream):
 
 
 def measure_variants(lib, renderer, textures, w, h, flush, stream, with_oracle, net, training):
-    """BASELINE's metric itself: the 3840x2160 sweep for each variant of the march -- plain with
+    """The benchmark metric itself: the 3840x2160 sweep for each variant of the march -- plain with
     UNORM8 (the reference's texel format), FP16 (also with the large-step coverage test in half2)
     or BF16 density textures, and the learned
     sun-cone surrogate with UNORM8 or FP16 density -- each with its ms/frame (CUDA events, L2 flushed

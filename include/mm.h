@@ -31,7 +31,7 @@ typedef enum mm_status {
     MM_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad size, bad enum, wrong texture shape */
     MM_ERR_CUDA = 2,             /* a CUDA runtime call failed (text in mm_last_error_string) */
     MM_ERR_OUT_OF_MEMORY = 3,    /* a device or host allocation failed */
-    MM_ERR_UNSUPPORTED = 4,      /* valid request this build does not implement */
+    MM_ERR_UNSUPPORTED = 4,      /* valid request the library does not implement */
     MM_ERR_TIMEOUT = 5,          /* a bounded device-side wait gave up */
     MM_ERR_NO_DEVICE = 6         /* no usable CUDA device */
 } mm_status;

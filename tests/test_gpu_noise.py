@@ -21,7 +21,7 @@ def test_noise_matches_oracle(cuda, mmlib, orc, kind, seed, size, ch):
     want = orc.noise(kind, seed, w, h, d, ch)
     diff = np.abs(got.astype(int) - want.astype(int))
     assert diff.max() <= 1  # gate: 8-bit texels within 1 LSB
-    assert np.array_equal(got, want)  # this build: identical
+    assert np.array_equal(got, want)  # measured identical
 
 
 def test_ref_curl_matches_shipped_texture(cuda, mmlib):

@@ -31,6 +31,32 @@
 #include "../project-marshmallow_gb300/csrc/mm_math.h"
 #include "oracle_glsl.h"
 
+// Per-iteration event trace (built into _build/liboracle_trace.so only, -DORACLE_TRACE): one byte
+// per iteration of the march loop of every traced pixel -- 1 large step without density, 2 large step
+// with density (step back, :428-434), 3 small step without density, 4 small step eroded below 1e-4 by
+// cloudHiRes (:437), 5 accumulated sample (sun cone, :441-466).  oracle/lane_model.py groups the
+// traces into the GPU kernel's warp tiles to model lane utilization.
+#ifdef ORACLE_TRACE
+static uint8_t* g_trace = nullptr;
+static size_t g_trace_cap = 0;
+static thread_local uint8_t* t_trace = nullptr;
+static thread_local size_t t_trace_n = 0;
+static inline void trace_event(int e) {
+    if (t_trace && t_trace_n < g_trace_cap) t_trace[t_trace_n++] = (uint8_t)e;
+}
+static inline void trace_pixel(size_t o) {
+    t_trace = g_trace ? g_trace + o * g_trace_cap : nullptr;
+    t_trace_n = 0;
+}
+extern "C" void oracle_trace_set(uint8_t* buf, size_t cap_per_pixel) {
+    g_trace = buf;
+    g_trace_cap = cap_per_pixel;
+}
+#else
+static inline void trace_event(int) {}
+static inline void trace_pixel(size_t) {}
+#endif
+
 namespace {
 
 // ---------------------------------------------------------------------------------- the pass
@@ -290,10 +316,14 @@ struct March {
                     t -= stepSize;
                     stepSize *= T(0.3);
                     noHits = false;
+                    trace_event(2);
                     continue;
                 }
                 density = cloudHiRes(pos + windOffset, stepSize, density, rh);
-                if (density < T(0.0001)) continue;
+                if (density < T(0.0001)) {
+                    trace_event(4);
+                    continue;
+                }
                 T densityAlongLight = T(0);
                 for (int i = 0; i < 6; i++) {
                     V3<T> lsPos = pos + T(3) * stepSize * samples[i];
@@ -315,7 +345,8 @@ struct March {
                 cnt->accumulated++;
                 if (firstT == std::numeric_limits<float>::infinity()) firstT = (float)t;
                 accum += density;
-            } else if (!noHits) {
+                trace_event(5);
+            } else if (trace_event(noHits ? 1 : 3), !noHits) {
                 misses++;
                 if (misses >= 10) {
                     noHits = true;
@@ -386,6 +417,7 @@ int run(const mm_uniforms* u, const oracle_textures* t, const oracle_frame* f, f
                 if (f->pixel_mode == MM_PIXELS_PHASE16 && ((px & 3) != (phase % 4) || (py & 3) != (phase / 4)))
                     continue;
                 size_t o = (size_t)r * cols + c;
+                trace_pixel(o);
                 m.pixel(px, py, uv_w, uv_h, out_rgba + 4 * o, out_depth ? out_depth + o : nullptr);
             }
         }

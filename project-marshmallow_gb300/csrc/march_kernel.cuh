@@ -21,11 +21,12 @@
 #include "mm_internal.h"
 #include "mm_math.h"
 
-// Build knobs (defaults measured best on GB300 at 3840x2160): warps per block of the tiled kernel
-// (4 or 8) and the minimum resident blocks per SM requested from the register allocator for it
-// (4 warps x 10 blocks: 48 registers, no spills, 40 warps per SM; 9 blocks / 56 registers was 4.6%
-// slower, 11 blocks spills); the same for the persistent kernel; and the speculative curl fetch of
-// the tiled march (off: it costs more occupancy than it hides).
+// Build knobs (defaults measured best on GB300 at 3840x2160): warps per block of the tiled kernels
+// (4 or 8) and the minimum resident blocks per SM requested from the register allocator for them
+// (4 warps x 10 blocks: 48 registers, 40 warps per SM; the inline-cone kernel has no spills there and
+// was 4.6% slower at 9 blocks / 56 registers; the pooled-cone kernel spills 64 B in its cone rounds
+// and was 2.6% / 5.1% slower at 9 / 11 blocks); the same for the persistent kernel; and the
+// speculative curl fetch of the tiled march (off: it costs more occupancy than it hides).
 #ifndef MM_TILED_WARPS
 #define MM_TILED_WARPS 4
 #endif
